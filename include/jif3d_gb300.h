@@ -1,0 +1,132 @@
+/*
+ * jif3d_gb300.h -- C ABI of the GB300 gravity / FTG / magnetic prism engine.
+ *
+ * One opaque context per implementation object, bound to one CUDA device and
+ * one stream.  Every call returns an int status (J3G_OK on success) and never
+ * exits the process; j3g_last_error() gives the message of the last failure.
+ * Calls on one context are not thread-safe (one caller at a time), as the
+ * reference's CUDA layer is not (Gravity/GravityInterface.h:19-20).
+ *
+ * Conventions (identical to jif3D, so no transposes are needed):
+ *   model cell (xi, yi, zi) at offset (xi*ny + yi)*nz + zi, z fastest, z down
+ *     (ModelBase/ThreeDModelBase.h:157-168);
+ *   model vectors hold ngrid grid values followed by nbg background values
+ *     (Gravity/ThreeDGravityModel.h:91-99);
+ *   raw data per station: scalar 1 (g_z), tensor 9 (Uxx..Uzz, C order),
+ *     magnetic 3 (Bx, By, Bz), joint 10 (g_z then the 9 tensor values);
+ *   sensitivity rows are row-major, nmeas*raw rows of ngrid+nbg columns
+ *     (GravMag/FullSensitivityGravMagCalculator.h:116-130);
+ *   angles in radians, field strength in nT, densities in kg/m^3, SI output.
+ *
+ * Pointer arguments named h_* are host memory; d_* are device memory of the
+ * context's device.
+ */
+#ifndef JIF3D_GB300_H_
+#define JIF3D_GB300_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct j3g_context j3g_context;
+
+enum j3g_status {
+  J3G_OK = 0,
+  J3G_ERR_ARG = 1,         /* bad argument or size */
+  J3G_ERR_CUDA = 2,        /* CUDA runtime error (message in j3g_last_error) */
+  J3G_ERR_NOMEM = 3,       /* device or host allocation failed */
+  J3G_ERR_STATE = 4,       /* call made before the mesh / stations / kind were set */
+  J3G_ERR_UNSUPPORTED = 5  /* combination not supported (e.g. I2 transform on scalar data) */
+};
+
+enum j3g_kind {
+  J3G_SCALAR = 1,   /* g_z,             ScalarOMPGravityImp / ScalarCudaGravityImp */
+  J3G_TENSOR = 2,   /* FTG 9 components, TensorOMPGravityImp / TensorCudaGravityImp */
+  J3G_MAGNETIC = 3, /* induced B,        OMPMagneticSusceptibilityImp / CudaMagneticSusceptibilityImp */
+  J3G_JOINT = 4     /* g_z + FTG in one pass (no single reference counterpart) */
+};
+
+enum j3g_transform {
+  J3G_T_NONE = 0,
+  J3G_T_FTG_INVARIANT = 1, /* FTGInvariant, Gravity/GravityTransforms.h:25-100 */
+  J3G_T_TOTAL_FIELD = 2,   /* TotalField, Magnetics/MagneticTransforms.h:19-82 */
+  J3G_T_TFA = 3            /* TotalFieldAnomaly, Magnetics/MagneticTransforms.h:84-156 */
+};
+
+/* Text of a status code. */
+const char *j3g_status_string(int status);
+/* Message of the last failing call on ctx (empty string if none). */
+const char *j3g_last_error(const j3g_context *ctx);
+
+/* Create a context on CUDA device `device` with its own stream.  Replaces the
+ * device probing of PrepareData (Gravity/gravcuda.cu:38-77), minus its exit()
+ * calls and its search for an unused device. */
+int j3g_create(j3g_context **ctx, int device);
+/* Free every device buffer of ctx.  Replaces FreeData (Gravity/gravcuda.cu:8-26);
+ * it never resets the device (the reference destructors call cudaDeviceReset,
+ * ScalarCudaGravityImp.cpp:52). */
+int j3g_destroy(j3g_context *ctx);
+/* Launch on a caller-owned stream (cudaStream_t passed as void*; NULL restores
+ * the context's own stream). */
+int j3g_set_stream(j3g_context *ctx, void *stream);
+
+/* Mesh: corner coordinates (n+1 values each, ThreeDModelBase::GetXCoordinates)
+ * and cell sizes (n values each).  Replaces the allocation and H2D copies of
+ * PrepareData (Gravity/gravcuda.cu:79-106). */
+int j3g_set_mesh(j3g_context *ctx, int nx, int ny, int nz, const double *h_xcoord,
+                 const double *h_ycoord, const double *h_zcoord, const double *h_xsize,
+                 const double *h_ysize, const double *h_zsize);
+/* Background layer thicknesses (ThreeDGravityModel::GetBackgroundThicknesses);
+ * the layer densities / susceptibilities are the last nbg model values. */
+int j3g_set_background(j3g_context *ctx, int nbg, const double *h_thick);
+/* Measurement positions (GeneralData::GetMeasPosX/Y/Z). */
+int j3g_set_stations(j3g_context *ctx, int nmeas, const double *h_x, const double *h_y,
+                     const double *h_z);
+/* Kind of data and, for J3G_MAGNETIC, the inducing field: inclination and
+ * declination in radians, field strength in nT
+ * (OMPMagneticSusceptibilityImp(Inc, Dec, Fs), Magnetics/OMPMagneticSusceptibilityImp.cpp:196). */
+int j3g_set_kind(j3g_context *ctx, int kind, double inclination, double declination,
+                 double field_strength);
+/* Output transform (ThreeDGravMagImplementation::SetDataTransform,
+ * GravMag/ThreeDGravMagImplementation.h:67-70); angles used by J3G_T_TFA. */
+int j3g_set_transform(j3g_context *ctx, int transform, double inclination, double declination);
+/* Sizes implied by the current setup (any pointer may be NULL). */
+int j3g_get_sizes(const j3g_context *ctx, long long *ngrid, long long *nparm, int *nmeas,
+                  int *raw_per_meas, int *data_per_meas);
+
+/* Forward response of all stations (host buffers): model nparm values ->
+ * data nmeas*data_per_meas values.  Matrix-free, no sensitivities kept.
+ * Replaces ThreeDGravMagImplementation::Calculate
+ * (GravMag/ThreeDGravMagImplementation.h:116-168) driven by
+ * MinMemGravMagCalculator, and the per-station SingleScalarMeas /
+ * SingleFTGMeas launches (Gravity/gravcuda.cu:117-197). */
+int j3g_forward(j3g_context *ctx, const double *h_model, double *h_data);
+/* As j3g_forward, and also the raw sensitivity rows (nmeas*raw x nparm,
+ * row-major) that FullSensitivityGravMagCalculator stores through
+ * HandleSensitivities (GravMag/FullSensitivityGravMagCalculator.h:98-130).
+ * The data are formed from the rows, cell by cell, as CalcGridded does. */
+int j3g_forward_sens(j3g_context *ctx, const double *h_model, double *h_data, double *h_sens);
+/* Least-squares derivative 2 * J^T (T' misfit), length nparm, computed
+ * matrix-free (box terms recomputed, nothing stored).  misfit has
+ * nmeas*data_per_meas values (already C_d^-1 weighted).  Replaces
+ * ThreeDGravMagImplementation::LQDerivative (GravMag/ThreeDGravMagImplementation.h:177-231). */
+int j3g_lqderivative(j3g_context *ctx, const double *h_model, const double *h_misfit,
+                     double *h_grad);
+
+/* Device-resident variants of j3g_forward / j3g_lqderivative (pointers on
+ * the context's device, work queued on the context's stream; no host sync). */
+int j3g_forward_device(j3g_context *ctx, const double *d_model, double *d_data);
+int j3g_lqderivative_device(j3g_context *ctx, const double *d_model, const double *d_misfit,
+                            double *d_grad);
+
+/* Block until the context's stream is idle. */
+int j3g_synchronize(j3g_context *ctx);
+
+/* Measured FP64 FMA rate of the device in GFLOP/s (2 flops per FMA), from a
+ * dependent-chain probe kernel; used for the FP64 roofline. */
+int j3g_probe_fp64(j3g_context *ctx, double *gflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JIF3D_GB300_H_ */

@@ -1,0 +1,199 @@
+"""ctypes binding of the C ABI in ``include/jif3d_gb300.h``.
+
+The library must have been built (``python -m jif3d_gb300.build`` or
+``__graft_entry__.build()``); there is no CPU fallback, a missing library or a
+missing GPU raises :class:`J3GError`.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_UNSUPPORTED = range(6)
+SCALAR, TENSOR, MAGNETIC, JOINT = 1, 2, 3, 4
+T_NONE, T_FTG_INVARIANT, T_TOTAL_FIELD, T_TFA = 0, 1, 2, 3
+
+_P = ctypes.POINTER(ctypes.c_double)
+_VP = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+_LL = ctypes.c_longlong
+
+# name -> (restype, argtypes); every function declared in include/jif3d_gb300.h
+SIGNATURES = {
+    "j3g_status_string": (ctypes.c_char_p, [_I]),
+    "j3g_last_error": (ctypes.c_char_p, [_VP]),
+    "j3g_create": (_I, [ctypes.POINTER(_VP), _I]),
+    "j3g_destroy": (_I, [_VP]),
+    "j3g_set_stream": (_I, [_VP, _VP]),
+    "j3g_set_mesh": (_I, [_VP, _I, _I, _I, _P, _P, _P, _P, _P, _P]),
+    "j3g_set_background": (_I, [_VP, _I, _P]),
+    "j3g_set_stations": (_I, [_VP, _I, _P, _P, _P]),
+    "j3g_set_kind": (_I, [_VP, _I, _D, _D, _D]),
+    "j3g_set_transform": (_I, [_VP, _I, _D, _D]),
+    "j3g_get_sizes": (_I, [_VP, ctypes.POINTER(_LL), ctypes.POINTER(_LL), ctypes.POINTER(_I),
+                           ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    "j3g_forward": (_I, [_VP, _P, _P]),
+    "j3g_forward_sens": (_I, [_VP, _P, _P, _P]),
+    "j3g_lqderivative": (_I, [_VP, _P, _P, _P]),
+    "j3g_forward_device": (_I, [_VP, _VP, _VP]),
+    "j3g_lqderivative_device": (_I, [_VP, _VP, _VP, _VP]),
+    "j3g_synchronize": (_I, [_VP]),
+    "j3g_probe_fp64": (_I, [_VP, _P]),
+}
+
+_lib = None
+
+
+class J3GError(RuntimeError):
+    def __init__(self, code, msg=""):
+        self.code = code
+        super().__init__(f"jif3d_gb300 error {code}: {msg}")
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load():
+    """Load libjif3d_gb300.so (raises J3GError if it has not been built)."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise J3GError(ERR_STATE, f"{path} is missing: build it with "
+                                      "`python -m jif3d_gb300.build`")
+        lib = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_P)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Context:
+    """One engine context on one device (owns its device buffers)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        h = _VP()
+        rc = self._lib.j3g_create(ctypes.byref(h), int(device))
+        if rc != OK:
+            raise J3GError(rc, "j3g_create failed: " +
+                           self._lib.j3g_status_string(rc).decode() +
+                           " (a CUDA device is required; there is no CPU fallback)")
+        self._h = h
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.j3g_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _check(self, rc):
+        if rc != OK:
+            msg = self._lib.j3g_last_error(self._h)
+            raise J3GError(rc, (msg or b"").decode() or
+                           self._lib.j3g_status_string(rc).decode())
+
+    # -- setup ---------------------------------------------------------------
+    def set_stream(self, stream_ptr):
+        self._check(self._lib.j3g_set_stream(self._h, _VP(stream_ptr) if stream_ptr else None))
+
+    def set_mesh(self, xcoord, ycoord, zcoord, xsize, ysize, zsize):
+        xs, ys, zs = _f64(xsize), _f64(ysize), _f64(zsize)
+        xc, yc, zc = _f64(xcoord), _f64(ycoord), _f64(zcoord)
+        self._check(self._lib.j3g_set_mesh(self._h, xs.size, ys.size, zs.size, _ptr(xc),
+                                           _ptr(yc), _ptr(zc), _ptr(xs), _ptr(ys), _ptr(zs)))
+
+    def set_background(self, thick):
+        t = _f64(thick)
+        self._check(self._lib.j3g_set_background(self._h, t.size, _ptr(t) if t.size else None))
+
+    def set_stations(self, x, y, z):
+        x, y, z = _f64(x), _f64(y), _f64(z)
+        self._check(self._lib.j3g_set_stations(self._h, x.size, _ptr(x), _ptr(y), _ptr(z)))
+
+    def set_kind(self, kind, inclination=0.0, declination=0.0, field_strength=0.0):
+        self._check(self._lib.j3g_set_kind(self._h, kind, inclination, declination,
+                                           field_strength))
+
+    def set_transform(self, transform, inclination=0.0, declination=0.0):
+        self._check(self._lib.j3g_set_transform(self._h, transform, inclination, declination))
+
+    def sizes(self):
+        ng, npar = _LL(), _LL()
+        nm, raw, dpm = _I(), _I(), _I()
+        self._check(self._lib.j3g_get_sizes(self._h, ctypes.byref(ng), ctypes.byref(npar),
+                                            ctypes.byref(nm), ctypes.byref(raw),
+                                            ctypes.byref(dpm)))
+        return dict(ngrid=ng.value, nparm=npar.value, nmeas=nm.value, raw=raw.value,
+                    dpm=dpm.value)
+
+    # -- compute (host buffers) ---------------------------------------------
+    def forward(self, model):
+        s = self.sizes()
+        m = _f64(model)
+        if m.size != s["nparm"]:
+            raise J3GError(ERR_ARG, f"model has {m.size} values, expected {s['nparm']}")
+        d = np.zeros(s["nmeas"] * s["dpm"])
+        self._check(self._lib.j3g_forward(self._h, _ptr(m), _ptr(d)))
+        return d
+
+    def forward_sens(self, model):
+        s = self.sizes()
+        m = _f64(model)
+        if m.size != s["nparm"]:
+            raise J3GError(ERR_ARG, f"model has {m.size} values, expected {s['nparm']}")
+        d = np.zeros(s["nmeas"] * s["dpm"])
+        J = np.zeros((s["nmeas"] * s["raw"], s["nparm"]))
+        self._check(self._lib.j3g_forward_sens(self._h, _ptr(m), _ptr(d), _ptr(J)))
+        return d, J
+
+    def lqderivative(self, model, misfit):
+        s = self.sizes()
+        m, r = _f64(model), _f64(misfit)
+        if m.size != s["nparm"] or r.size != s["nmeas"] * s["dpm"]:
+            raise J3GError(ERR_ARG, "model or misfit size mismatch")
+        g = np.zeros(s["nparm"])
+        self._check(self._lib.j3g_lqderivative(self._h, _ptr(m), _ptr(r), _ptr(g)))
+        return g
+
+    # -- compute (device pointers, e.g. torch tensors' data_ptr()) -----------
+    def forward_device(self, d_model, d_data):
+        self._check(self._lib.j3g_forward_device(self._h, _VP(d_model), _VP(d_data)))
+
+    def lqderivative_device(self, d_model, d_misfit, d_grad):
+        self._check(self._lib.j3g_lqderivative_device(self._h, _VP(d_model), _VP(d_misfit),
+                                                      _VP(d_grad)))
+
+    def synchronize(self):
+        self._check(self._lib.j3g_synchronize(self._h))
+
+    def probe_fp64(self):
+        v = _D()
+        self._check(self._lib.j3g_probe_fp64(self._h, ctypes.byref(v)))
+        return v.value

@@ -1,0 +1,540 @@
+"""Python host layer mirroring jif3D's gravity / magnetic plugin interface.
+
+Names, argument meaning and error behaviour follow the reference classes so
+that code (and tests) written against jif3D read the same here:
+
+* models  -- ``ThreeDGravityModel`` / ``ThreeDSusceptibilityModel``
+  (ModelBase/ThreeDModelBase.h, Gravity/ThreeDGravityModel.h,
+  Magnetics/ThreeDSusceptibilityModel.h)
+* data    -- ``ScalarGravityData``, ``TensorGravityData``,
+  ``TotalFieldMagneticData`` (DataBase/GeneralData.h)
+* transforms -- ``FTGInvariant``, ``TotalField``, ``TotalFieldAnomaly``
+  (Gravity/GravityTransforms.h, Magnetics/MagneticTransforms.h)
+* implementations -- ``ScalarGB300GravityImp``, ``TensorGB300GravityImp``,
+  ``GB300MagneticSusceptibilityImp``, ``JointGB300GravityImp``: the GB300
+  counterparts of the ThreeDGravMagImplementation subclasses
+  (GravMag/ThreeDGravMagImplementation.h:39-84)
+* calculators -- ``MinMemGravMagCalculator``, ``FullSensitivityGravMagCalculator``
+  (GravMag/MinMemGravMagCalculator.h, GravMag/FullSensitivityGravMagCalculator.h),
+  unchanged in behaviour: they drive the implementation exactly as the
+  reference calculators drive theirs.
+
+Every computation runs on the GPU through the C ABI (``capi``); the
+calculators' cached products (J m, 2 J^T r) are the reference's host-side
+products, as in FullSensitivityGravMagCalculator.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import capi
+
+
+class FatalException(RuntimeError):
+    """jif3D::FatalException (Global/FatalException.h:27)."""
+
+
+# ---------------------------------------------------------------------------
+# Models and data
+class ThreeDModelBase:
+    """Rectilinear mesh, z fastest, z positive down (ModelBase/ThreeDModelBase.h)."""
+
+    def __init__(self):
+        self._xs = np.zeros(0)
+        self._ys = np.zeros(0)
+        self._zs = np.zeros(0)
+        self._origin = np.zeros(3)
+        self._data = np.zeros((0, 0, 0))
+        self._bg_values = np.zeros(0)
+        self._bg_thick = np.zeros(0)
+
+    # mesh -------------------------------------------------------------------
+    def SetMeshSize(self, nx, ny, nz):
+        self._xs = np.resize(self._xs, nx).astype(float)
+        self._ys = np.resize(self._ys, ny).astype(float)
+        self._zs = np.resize(self._zs, nz).astype(float)
+        self._data = np.zeros((nx, ny, nz))
+
+    def SetXCellSizes(self, v):
+        self._xs = np.array(v, dtype=float)
+
+    def SetYCellSizes(self, v):
+        self._ys = np.array(v, dtype=float)
+
+    def SetZCellSizes(self, v):
+        self._zs = np.array(v, dtype=float)
+
+    def SetOrigin(self, x, y, z):
+        self._origin = np.array([x, y, z], dtype=float)
+
+    def GetXCellSizes(self):
+        return self._xs
+
+    def GetYCellSizes(self):
+        return self._ys
+
+    def GetZCellSizes(self):
+        return self._zs
+
+    @staticmethod
+    def _coords(origin, sizes):
+        # ThreeDModelBase::CalcCoords (ModelBase/ThreeDModelBase.cpp:96-113):
+        # running sum of the sizes, in order, starting at the origin
+        c = np.empty(sizes.size + 1)
+        c[0] = origin
+        s = origin
+        for i, v in enumerate(sizes):
+            s = s + v
+            c[i + 1] = s
+        return c
+
+    def GetXCoordinates(self):
+        return self._coords(self._origin[0], self._xs)
+
+    def GetYCoordinates(self):
+        return self._coords(self._origin[1], self._ys)
+
+    def GetZCoordinates(self):
+        return self._coords(self._origin[2], self._zs)
+
+    def GetXOrigin(self):
+        return float(self._origin[0])
+
+    def GetYOrigin(self):
+        return float(self._origin[1])
+
+    def GetZOrigin(self):
+        return float(self._origin[2])
+
+    # values -----------------------------------------------------------------
+    def SetData(self):
+        return self._data
+
+    def GetData(self):
+        return self._data
+
+    def SetBackgroundThicknesses(self, v):
+        self._bg_thick = np.array(v, dtype=float)
+
+    def GetBackgroundThicknesses(self):
+        return self._bg_thick
+
+    def SetBackgroundValues(self, v):
+        self._bg_values = np.array(v, dtype=float)
+
+    def GetBackgroundValues(self):
+        return self._bg_values
+
+    def GetModelParameters(self):
+        """Grid values followed by the background values (ThreeDGravityModel.h:91-99)."""
+        return np.concatenate([self._data.reshape(-1), self._bg_values])
+
+    def GetNModelParm(self):
+        return self._data.size + self._bg_values.size
+
+    def GetNModelElements(self):
+        return self._data.size
+
+
+class ThreeDGravityModel(ThreeDModelBase):
+    SetDensities = ThreeDModelBase.SetData
+    GetDensities = ThreeDModelBase.GetData
+    SetBackgroundDensities = ThreeDModelBase.SetBackgroundValues
+    GetBackgroundDensities = ThreeDModelBase.GetBackgroundValues
+
+
+class ThreeDSusceptibilityModel(ThreeDModelBase):
+    SetSusceptibilities = ThreeDModelBase.SetData
+    GetSusceptibilities = ThreeDModelBase.GetData
+    SetBackgroundSusceptibilities = ThreeDModelBase.SetBackgroundValues
+    GetBackgroundSusceptibilities = ThreeDModelBase.GetBackgroundValues
+
+
+class GeneralData:
+    """Measurement positions (DataBase/GeneralData.h)."""
+
+    def __init__(self):
+        self._x, self._y, self._z = [], [], []
+
+    def AddMeasurementPoint(self, x, y, z):
+        self._x.append(float(x))
+        self._y.append(float(y))
+        self._z.append(float(z))
+
+    def GetMeasPosX(self):
+        return np.array(self._x)
+
+    def GetMeasPosY(self):
+        return np.array(self._y)
+
+    def GetMeasPosZ(self):
+        return np.array(self._z)
+
+    def CopyMeasurementConfiguration(self, other):
+        self._x, self._y, self._z = list(other._x), list(other._y), list(other._z)
+
+    def ClearMeasurementPoints(self):
+        self._x, self._y, self._z = [], [], []
+
+
+class ScalarGravityData(GeneralData):
+    ModelType = ThreeDGravityModel
+
+
+class TensorGravityData(GeneralData):
+    ModelType = ThreeDGravityModel
+
+
+class TotalFieldMagneticData(GeneralData):
+    ModelType = ThreeDSusceptibilityModel
+
+
+# ---------------------------------------------------------------------------
+# Transforms (host-side Transform / Derivative used by the cached calculator
+# path, exactly as VectorTransform is used there)
+class VectorTransform:
+    code = capi.T_NONE
+    inclination = 0.0
+    declination = 0.0
+
+
+class FTGInvariant(VectorTransform):
+    """I2 invariant, Gravity/GravityTransforms.h:25-100."""
+    code = capi.T_FTG_INVARIANT
+
+    def GetInputSize(self):
+        return 9
+
+    def GetOutputSize(self):
+        return 1
+
+    def Transform(self, d):
+        return np.array([d[0] * d[4] + d[4] * d[8] + d[0] * d[8] - d[3] * d[1] - d[7] * d[5]
+                         - d[2] * d[6]])
+
+    def Derivative(self, d):
+        return np.array([[d[4] + d[8], -d[3], -d[6], -d[1], d[0] + d[8], -d[7], -d[2], -d[5],
+                          d[0] + d[4]]])
+
+
+class TotalField(VectorTransform):
+    """|B|, Magnetics/MagneticTransforms.h:19-82."""
+    code = capi.T_TOTAL_FIELD
+
+    def GetInputSize(self):
+        return 3
+
+    def GetOutputSize(self):
+        return 1
+
+    def Transform(self, d):
+        return np.array([np.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])])
+
+    def Derivative(self, d):
+        t = np.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+        return np.array([[d[0] / t, d[1] / t, d[2] / t]])
+
+
+class TotalFieldAnomaly(VectorTransform):
+    """Projection on the inducing field, Magnetics/MagneticTransforms.h:84-156."""
+    code = capi.T_TFA
+
+    def __init__(self, inc=0.0, dec=0.0):
+        self.inclination = float(inc)
+        self.declination = float(dec)
+        self._b = np.array([np.cos(inc) * np.cos(dec), np.cos(inc) * np.sin(dec), np.sin(inc)])
+
+    def GetInputSize(self):
+        return 3
+
+    def GetOutputSize(self):
+        return 1
+
+    def Transform(self, d):
+        return np.array([self._b[0] * d[0] + self._b[1] * d[1] + self._b[2] * d[2]])
+
+    def Derivative(self, d):
+        return self._b.reshape(1, 3).copy()
+
+
+def ApplyTransform(data, transform):
+    """Global/VectorTransform.h:158-181."""
+    step, nout = transform.GetInputSize(), transform.GetOutputSize()
+    if data.size % step:
+        raise FatalException("Transformation size needs to be integer multiple of input "
+                             "data size")
+    out = np.empty(data.size // step * nout)
+    for i in range(0, data.size, step):
+        out[i // step * nout:(i // step + 1) * nout] = transform.Transform(data[i:i + step])
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Implementations
+class GB300GravMagImplementation:
+    """GB300 counterpart of jif3D::ThreeDGravMagImplementation.
+
+    Calculate and LQDerivative are overridden as whole-survey calls into the
+    C ABI; the per-station obligations of the base class (fill the calculator's
+    current sensitivities when they are large enough, call
+    HandleSensitivities(i) in station order, store raw sensitivities) are kept.
+    """
+
+    KIND = None
+
+    def __init__(self, device=0):
+        self._device = device
+        self._ctx = None
+        self._key = None
+        self.Transform = None
+
+    def _context(self):
+        if self._ctx is None:
+            self._ctx = capi.Context(self._device)
+        return self._ctx
+
+    def RawDataPerMeasurement(self):
+        return {capi.SCALAR: 1, capi.TENSOR: 9, capi.MAGNETIC: 3, capi.JOINT: 10}[self.KIND]
+
+    def SetDataTransform(self, transform):
+        self.Transform = transform
+
+    def GetDataPerMeasurement(self):
+        return self.Transform.GetOutputSize() if self.Transform else self.RawDataPerMeasurement()
+
+    def _kind_args(self):
+        return (self.KIND, 0.0, 0.0, 0.0)
+
+    def _prepare(self, Model, Data):
+        ctx = self._context()
+        key = (self.GetDataPerMeasurement(), self._kind_args(),
+               self.Transform.code if self.Transform else 0,
+               getattr(self.Transform, "inclination", 0.0),
+               getattr(self.Transform, "declination", 0.0),
+               Model.GetXOrigin(), Model.GetYOrigin(), Model.GetZOrigin(),
+               Model.GetXCellSizes().tobytes(), Model.GetYCellSizes().tobytes(),
+               Model.GetZCellSizes().tobytes(), Model.GetBackgroundThicknesses().tobytes(),
+               Data.GetMeasPosX().tobytes(), Data.GetMeasPosY().tobytes(),
+               Data.GetMeasPosZ().tobytes())
+        if key != self._key:
+            ctx.set_mesh(Model.GetXCoordinates(), Model.GetYCoordinates(),
+                         Model.GetZCoordinates(), Model.GetXCellSizes(), Model.GetYCellSizes(),
+                         Model.GetZCellSizes())
+            ctx.set_background(Model.GetBackgroundThicknesses())
+            ctx.set_stations(Data.GetMeasPosX(), Data.GetMeasPosY(), Data.GetMeasPosZ())
+            ctx.set_kind(*self._kind_args())
+            t = self.Transform
+            ctx.set_transform(t.code if t else capi.T_NONE, getattr(t, "inclination", 0.0),
+                              getattr(t, "declination", 0.0))
+            self._key = key
+        return ctx
+
+    def Calculate(self, Model, Data, Calculator):
+        """ThreeDGravMagImplementation::Calculate (ThreeDGravMagImplementation.h:116-168)."""
+        ctx = self._prepare(Model, Data)
+        model = Model.GetModelParameters()
+        nmeas = Data.GetMeasPosX().size
+        raw = self.RawDataPerMeasurement()
+        cur = Calculator.SetCurrentSensitivities()
+        wants_rows = cur.shape[0] >= raw and cur.shape[1] >= Model.GetNModelParm() \
+            and Model.GetNModelElements() > 0
+        if not wants_rows:
+            return ctx.forward(model)
+        data, J = ctx.forward_sens(model)
+        ncol = Model.GetNModelParm()
+        for i in range(nmeas):
+            cur[:raw, :ncol] = J[i * raw:(i + 1) * raw]
+            Calculator.HandleSensitivities(i)
+        return data
+
+    def LQDerivative(self, Model, Data, Misfit):
+        """Matrix-free 2 J^T (T' misfit) (ThreeDGravMagImplementation.h:177-231)."""
+        ctx = self._prepare(Model, Data)
+        misfit = np.asarray(Misfit, dtype=float)
+        if misfit.size != Data.GetMeasPosX().size * self.GetDataPerMeasurement():
+            raise FatalException("Misfit size does not match the number of data")
+        return ctx.lqderivative(Model.GetModelParameters(), misfit)
+
+
+class ScalarGB300GravityImp(GB300GravMagImplementation):
+    """Replaces ScalarOMPGravityImp / ScalarCudaGravityImp."""
+    KIND = capi.SCALAR
+
+
+class TensorGB300GravityImp(GB300GravMagImplementation):
+    """Replaces TensorOMPGravityImp / TensorCudaGravityImp."""
+    KIND = capi.TENSOR
+
+
+class JointGB300GravityImp(GB300GravMagImplementation):
+    """g_z and the 9 FTG values of each station in one pass (10 raw values)."""
+    KIND = capi.JOINT
+
+
+class GB300MagneticSusceptibilityImp(GB300GravMagImplementation):
+    """Replaces OMPMagneticSusceptibilityImp / CudaMagneticSusceptibilityImp.
+    Inclination and declination in radians, field strength in nT."""
+    KIND = capi.MAGNETIC
+
+    def __init__(self, Inc=0.0, Dec=0.0, Fs=1.0, device=0):
+        super().__init__(device)
+        self.Inclination, self.Declination, self.FieldStrength = float(Inc), float(Dec), float(Fs)
+
+    def _kind_args(self):
+        return (self.KIND, self.Inclination, self.Declination, self.FieldStrength)
+
+
+# ---------------------------------------------------------------------------
+# Calculators
+class ThreeDGravMagCalculator:
+    """GravMag/ThreeDGravMagCalculator.h:47-173."""
+
+    def __init__(self, imp):
+        self.Imp = imp
+        self.Transform = None
+        self._current = np.zeros((0, 0))
+
+    def SetDataTransform(self, transform):
+        self.Transform = transform
+        self.Imp.SetDataTransform(transform)
+
+    def GetDataPerMeasurement(self):
+        return self.Imp.GetDataPerMeasurement()
+
+    def SetCurrentSensitivities(self):
+        return self._current
+
+    def _resize_current(self, r, c):
+        self._current = np.zeros((r, c))
+
+    def CheckModelConsistency(self, Model):
+        shp = Model.GetData().shape
+        if shp[0] != Model.GetXCellSizes().size:
+            raise FatalException("Model x-dimension does not match size for specification of "
+                                 "cell sizes. ")
+        if shp[1] != Model.GetYCellSizes().size:
+            raise FatalException("Model y-dimension does not match size for specification of "
+                                 "cell sizes. ")
+        if shp[2] != Model.GetZCellSizes().size:
+            raise FatalException("Model x-dimension does not match size for specification of "
+                                 "cell sizes. ")
+
+    def Calculate(self, Model, Data):
+        self.CheckModelConsistency(Model)
+        return self.Imp.Calculate(Model, Data, self)
+
+    def LQDerivative(self, Model, Data, Misfit):
+        self.CheckModelConsistency(Model)
+        return self.Imp.LQDerivative(Model, Data, Misfit)
+
+    def HandleSensitivities(self, measindex):
+        raise NotImplementedError
+
+
+class MinMemGravMagCalculator(ThreeDGravMagCalculator):
+    """GravMag/MinMemGravMagCalculator.h: no sensitivities kept."""
+
+    def Calculate(self, Model, Data):
+        self._resize_current(0, 0)
+        return super().Calculate(Model, Data)
+
+    def HandleSensitivities(self, measindex):
+        pass
+
+
+class _GridBackgroundModelCache:
+    """ModelBase/GridBackgroundModelCache.h: cell sizes + background values and
+    thicknesses (station positions are not part of the key, as in the reference)."""
+
+    def __init__(self):
+        self._old = None
+
+    def HasChanged(self, Model):
+        new = (Model.GetXCellSizes().tobytes(), Model.GetYCellSizes().tobytes(),
+               Model.GetZCellSizes().tobytes(), Model.GetBackgroundValues().tobytes(),
+               Model.GetBackgroundThicknesses().tobytes())
+        changed = new != self._old
+        self._old = new
+        return changed
+
+
+class CachedGravMagCalculator(ThreeDGravMagCalculator):
+    """GravMag/CachedGravMagCalculator.h:28-143."""
+
+    def __init__(self, imp):
+        super().__init__(imp)
+        self._have_cache = False
+        self._cache = _GridBackgroundModelCache()
+
+    def InvalidateCache(self):
+        self._have_cache = False
+
+    def Calculate(self, Model, Data):
+        self.CheckModelConsistency(Model)
+        changed = self._cache.HasChanged(Model)
+        if self._have_cache and not changed:
+            return self.CalculateCachedResult(Model, Data)
+        self._resize_current(self.Imp.RawDataPerMeasurement(), Model.GetNModelParm())
+        result = self.CalculateNewModel(Model, Data)
+        self._have_cache = True
+        return result
+
+    def LQDerivative(self, Model, Data, Misfit):
+        self.CheckModelConsistency(Model)
+        changed = self._cache.HasChanged(Model)
+        if self._have_cache and not changed:
+            return self.CachedLQDerivative(Model, Data, Misfit)
+        self._resize_current(self.Imp.GetDataPerMeasurement(), Model.GetNModelParm())
+        return ThreeDGravMagCalculator.LQDerivative(self, Model, Data, Misfit)
+
+
+class FullSensitivityGravMagCalculator(CachedGravMagCalculator):
+    """GravMag/FullSensitivityGravMagCalculator.h:33-221 (J kept in host memory)."""
+
+    def __init__(self, imp):
+        super().__init__(imp)
+        self.Sensitivities = np.zeros((0, 0))
+
+    def GetSensitivities(self):
+        return self.Sensitivities
+
+    def SetSensitivities(self):
+        self.InvalidateCache()
+        return self.Sensitivities
+
+    def HandleSensitivities(self, measindex):
+        raw = self.Imp.RawDataPerMeasurement()
+        self.Sensitivities[measindex * raw:(measindex + 1) * raw, :] = \
+            self._current[:, :self.Sensitivities.shape[1]]
+
+    def CalculateNewModel(self, Model, Data):
+        nmeas = Data.GetMeasPosX().size
+        self.Sensitivities = np.zeros((nmeas * self.Imp.RawDataPerMeasurement(),
+                                       Model.GetNModelParm()))
+        return self.Imp.Calculate(Model, Data, self)
+
+    def CalculateRawData(self, Model, Data):
+        nrow = Data.GetMeasPosX().size * self.Imp.RawDataPerMeasurement()
+        if self.Sensitivities.shape != (nrow, Model.GetNModelParm()):
+            raise FatalException("Size of sensitivity matrix does not match model "
+                                 "configuration ! ")
+        return self.Sensitivities @ Model.GetModelParameters()
+
+    def CalculateCachedResult(self, Model, Data):
+        if self.Transform:
+            return ApplyTransform(self.CalculateRawData(Model, Data), self.Transform)
+        return self.CalculateRawData(Model, Data)
+
+    def CachedLQDerivative(self, Model, Data, Misfit):
+        result = self.CalculateRawData(Model, Data)
+        misfit = np.asarray(Misfit, dtype=float)
+        if not self.Transform:
+            processed = misfit
+        else:
+            nin, nout = self.Transform.GetInputSize(), self.Transform.GetOutputSize()
+            processed = np.empty(misfit.size // nout * nin)
+            for i in range(0, misfit.size, nout):
+                o = i // nout * nin
+                processed[o:o + nin] = self.Transform.Derivative(result[o:o + nin]).T @ \
+                    misfit[i:i + nout]
+        return 2.0 * (self.Sensitivities.T @ processed)

@@ -1,0 +1,3 @@
+// Stand-in for boost/numeric/ublas/matrix_sparse.hpp (oracle build only; not Boost code).
+#include "matrix.hpp"
+#include "vector.hpp"
