@@ -121,10 +121,16 @@ int j3g_lqderivative_device(j3g_context *ctx, const double *d_model, const doubl
 
 /* Block until the context's stream is idle. */
 int j3g_synchronize(j3g_context *ctx);
+/* Number of CUDA kernels this context has queued since it was created. */
+int j3g_launch_count(const j3g_context *ctx, long long *count);
 
 /* Measured FP64 FMA rate of the device in GFLOP/s (2 flops per FMA), from a
  * dependent-chain probe kernel; used for the FP64 roofline. */
 int j3g_probe_fp64(j3g_context *ctx, double *gflops);
+/* Launch the four libm probe kernels (loop only, sqrt, log, atan2; n_iter
+ * calls per thread) on `device`, for counting FP64 instructions per call with
+ * a profiler.  Measurement only; no counterpart in the reference. */
+int j3g_probe_math(int device, int n_iter);
 
 #ifdef __cplusplus
 }

@@ -43,7 +43,9 @@ SIGNATURES = {
     "j3g_forward_device": (_I, [_VP, _VP, _VP]),
     "j3g_lqderivative_device": (_I, [_VP, _VP, _VP, _VP]),
     "j3g_synchronize": (_I, [_VP]),
+    "j3g_launch_count": (_I, [_VP, ctypes.POINTER(_LL)]),
     "j3g_probe_fp64": (_I, [_VP, _P]),
+    "j3g_probe_math": (_I, [_I, _I]),
 }
 
 _lib = None
@@ -192,6 +194,11 @@ class Context:
 
     def synchronize(self):
         self._check(self._lib.j3g_synchronize(self._h))
+
+    def launch_count(self):
+        v = _LL()
+        self._check(self._lib.j3g_launch_count(self._h, ctypes.byref(v)))
+        return v.value
 
     def probe_fp64(self):
         v = _D()

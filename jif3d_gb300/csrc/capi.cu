@@ -50,6 +50,7 @@ struct j3g_context {
   int transform = J3G_T_NONE;
   double tinc = 0, tdec = 0;
   bool bg_dirty = true;
+  long long launches = 0;  // kernels queued by this context
 
   // device copies of the geometry
   DevBuf dX, dY, dZ, dxs, dys, dzs, dbg, dsx, dsy, dsz;
@@ -79,6 +80,15 @@ int cuda_fail(j3g_context *c, cudaError_t e, const char *where) {
   do {                                                      \
     cudaError_t e_ = (call);                                \
     if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+// A launcher call: check its error and count the kernels it queued (each
+// launcher queues one kernel; the two-kernel launchers add one more below).
+#define J3G_LAUNCH(ctx, call)                               \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    ++(ctx)->launches;                                      \
   } while (0)
 
 int ensure(j3g_context *c, DevBuf &b, size_t bytes) {
@@ -176,7 +186,7 @@ int ensure_background(j3g_context *c) {
   if (c->nmeas > 0) {
     // model origin = first corner coordinate (ThreeDModelBase::GetXOrigin)
     const double xo = c->X[0], yo = c->Y[0], zo = c->Z[0];
-    J3G_CUDA(c, launch_background(c->kind, mesh_view(c), station_view(c), nbg, ptr<double>(c->dbg),
+    J3G_LAUNCH(c, launch_background(c->kind, mesh_view(c), station_view(c), nbg, ptr<double>(c->dbg),
                                   xo, yo, zo, c->xw, c->yw, c->zw, mag_field(c),
                                   ptr<double>(c->bgsens), c->stream));
   }
@@ -191,7 +201,7 @@ int gridded_node_forward(j3g_context *c, const double *d_model) {
   const long long nn = c->nnodes();
   J3G_TRY(ensure(c, c->rhot, sizeof(double) * nn));
   MeshView m = mesh_view(c);
-  J3G_CUDA(c, launch_rho_tilde(m, d_model, ptr<double>(c->rhot), c->stream));
+  J3G_LAUNCH(c, launch_rho_tilde(m, d_model, ptr<double>(c->rhot), c->stream));
   int npb = 2048, spb = 4;
   auto blocks = [&](int a, int b) {
     return ((nn + a - 1) / a) * (long long)((c->nmeas + b - 1) / b);
@@ -202,9 +212,9 @@ int gridded_node_forward(j3g_context *c, const double *d_model) {
   const int ncomp = kind_ncomp(c->kind);
   J3G_TRY(ensure(c, c->partial, sizeof(double) * (size_t)nblk * c->nmeas * ncomp));
   J3G_TRY(ensure(c, c->comps, sizeof(double) * (size_t)c->nmeas * NC_COUNT));
-  J3G_CUDA(c, launch_node_forward(c->kind, m, station_view(c), ptr<double>(c->rhot),
+  J3G_LAUNCH(c, launch_node_forward(c->kind, m, station_view(c), ptr<double>(c->rhot),
                                   ptr<double>(c->partial), nblk, npb, spb, c->stream));
-  J3G_CUDA(c, launch_forward_reduce(c->kind, c->nmeas, nblk, ptr<double>(c->partial),
+  J3G_LAUNCH(c, launch_forward_reduce(c->kind, c->nmeas, nblk, ptr<double>(c->partial),
                                     ptr<double>(c->comps), c->stream));
   return J3G_OK;
 }
@@ -237,9 +247,10 @@ int gridded_rows_forward(j3g_context *c, const double *d_model, double *h_sens) 
   for (int s0 = 0; s0 < c->nmeas; s0 += chunk) {
     const int ns = std::min(chunk, c->nmeas - s0);
     if (ngrid > 0) {
-      J3G_CUDA(c, launch_sens_rows(c->kind, c->node_exact, m, s, s0, ns, mf, ptr<double>(c->F),
+      J3G_LAUNCH(c, launch_sens_rows(c->kind, c->node_exact, m, s, s0, ns, mf, ptr<double>(c->F),
                                    ptr<double>(c->rows), ld, c->stream));
-      J3G_CUDA(c, launch_rows_dot(raw, ns, ngrid, ptr<double>(c->rows), ld, d_model,
+      if (c->node_exact) ++c->launches;  // node terms + cell combine
+      J3G_LAUNCH(c, launch_rows_dot(raw, ns, ngrid, ptr<double>(c->rows), ld, d_model,
                                   ptr<double>(c->rowsum) + (size_t)s0 * raw, c->stream));
     } else {
       J3G_CUDA(c, cudaMemsetAsync(ptr<double>(c->rowsum) + (size_t)s0 * raw, 0,
@@ -273,7 +284,7 @@ int forward_device(j3g_context *c, const double *d_model, double *d_data, double
   const double *bgsens = nbg ? ptr<double>(c->bgsens) : nullptr;
   if (h_sens || (!c->node_exact && c->ngrid() > 0)) {
     J3G_TRY(gridded_rows_forward(c, d_model, h_sens));
-    J3G_CUDA(c, launch_assemble(c->kind, c->transform, tbx, tby, tbz, c->nmeas,
+    J3G_LAUNCH(c, launch_assemble(c->kind, c->transform, tbx, tby, tbz, c->nmeas,
                                 ptr<double>(c->rowsum), c->raw(), bgsens, nbg, bgval,
                                 mag_field(c), raw_out, d_data, c->stream));
   } else {
@@ -283,7 +294,7 @@ int forward_device(j3g_context *c, const double *d_model, double *d_data, double
       J3G_TRY(ensure(c, c->comps, sizeof(double) * (size_t)c->nmeas * NC_COUNT));
       J3G_CUDA(c, cudaMemsetAsync(c->comps.p, 0, sizeof(double) * c->nmeas * NC_COUNT, c->stream));
     }
-    J3G_CUDA(c, launch_assemble(c->kind, c->transform, tbx, tby, tbz, c->nmeas,
+    J3G_LAUNCH(c, launch_assemble(c->kind, c->transform, tbx, tby, tbz, c->nmeas,
                                 ptr<double>(c->comps), NC_COUNT, bgsens, nbg, bgval, mag_field(c),
                                 raw_out, d_data, c->stream));
   }
@@ -311,13 +322,13 @@ int adjoint_device(j3g_context *c, const double *d_model, const double *d_misfit
     rawd = ptr<double>(c->rawd);
   }
   J3G_TRY(ensure(c, c->wraw, sizeof(double) * (size_t)c->nmeas * raw));
-  J3G_CUDA(c, launch_backproject(c->kind, c->transform, tbx, tby, tbz, c->nmeas, d_misfit, rawd,
+  J3G_LAUNCH(c, launch_backproject(c->kind, c->transform, tbx, tby, tbz, c->nmeas, d_misfit, rawd,
                                  ptr<double>(c->wraw), c->stream));
   MeshView m = mesh_view(c);
   StationView s = station_view(c);
   if (ngrid > 0 && c->node_exact) {
     J3G_TRY(ensure(c, c->W, sizeof(double) * (size_t)c->nmeas * NC_COUNT));
-    J3G_CUDA(c, launch_comp_weights(c->kind, c->nmeas, ptr<double>(c->wraw), mag_field(c),
+    J3G_LAUNCH(c, launch_comp_weights(c->kind, c->nmeas, ptr<double>(c->wraw), mag_field(c),
                                     ptr<double>(c->W), c->stream));
     const long long nn = c->nnodes();
     const long long nodeblocks = (nn + 255) / 256;
@@ -328,10 +339,11 @@ int adjoint_device(j3g_context *c, const double *d_model, const double *d_misfit
     nchunk = (c->nmeas + spc - 1) / spc;
     J3G_TRY(ensure(c, c->Gpart, sizeof(double) * (size_t)nchunk * nn));
     J3G_TRY(ensure(c, c->G, sizeof(double) * (size_t)nn));
-    J3G_CUDA(c, launch_node_adjoint(c->kind, m, s, ptr<double>(c->W), spc, nchunk,
+    J3G_LAUNCH(c, launch_node_adjoint(c->kind, m, s, ptr<double>(c->W), spc, nchunk,
                                     ptr<double>(c->Gpart), c->stream));
-    J3G_CUDA(c, launch_adjoint_combine(m, nchunk, ptr<double>(c->Gpart), ptr<double>(c->G),
+    J3G_LAUNCH(c, launch_adjoint_combine(m, nchunk, ptr<double>(c->Gpart), ptr<double>(c->G),
                                        d_grad, c->stream));
+    ++c->launches;  // chunk sum + cell combine
   } else if (ngrid > 0) {
     // eight-corner rows, accumulated chunk by chunk
     J3G_CUDA(c, cudaMemsetAsync(d_grad, 0, sizeof(double) * (size_t)ngrid, c->stream));
@@ -340,15 +352,15 @@ int adjoint_device(j3g_context *c, const double *d_model, const double *d_misfit
     const MagField mf = mag_field(c);
     for (int s0 = 0; s0 < c->nmeas; s0 += chunk) {
       const int ns = std::min(chunk, c->nmeas - s0);
-      J3G_CUDA(c, launch_sens_rows(c->kind, false, m, s, s0, ns, mf, nullptr,
+      J3G_LAUNCH(c, launch_sens_rows(c->kind, false, m, s, s0, ns, mf, nullptr,
                                    ptr<double>(c->rows), ngrid, c->stream));
-      J3G_CUDA(c, launch_rows_tdot(ns * raw, ngrid, ptr<double>(c->rows), ngrid,
+      J3G_LAUNCH(c, launch_rows_tdot(ns * raw, ngrid, ptr<double>(c->rows), ngrid,
                                    ptr<double>(c->wraw) + (size_t)s0 * raw, d_grad, c->stream));
     }
-    J3G_CUDA(c, launch_scale(ngrid, 2.0, d_grad, c->stream));
+    J3G_LAUNCH(c, launch_scale(ngrid, 2.0, d_grad, c->stream));
   }
   if (nbg > 0)
-    J3G_CUDA(c, launch_background_grad(c->kind, c->nmeas, nbg, ptr<double>(c->wraw),
+    J3G_LAUNCH(c, launch_background_grad(c->kind, c->nmeas, nbg, ptr<double>(c->wraw),
                                        ptr<double>(c->bgsens), d_grad + ngrid, c->stream));
   return J3G_OK;
 }
@@ -595,6 +607,12 @@ int j3g_lqderivative(j3g_context *c, const double *h_model, const double *h_misf
   return J3G_OK;
 }
 
+int j3g_launch_count(const j3g_context *c, long long *count) {
+  if (!c || !count) return J3G_ERR_ARG;
+  *count = c->launches;
+  return J3G_OK;
+}
+
 int j3g_synchronize(j3g_context *c) {
   if (!c) return J3G_ERR_ARG;
   cudaSetDevice(c->device);
@@ -615,7 +633,7 @@ int j3g_probe_fp64(j3g_context *c, double *gflops) {
   float best = 1e30f;
   for (int rep = 0; rep < 4; ++rep) {
     J3G_CUDA(c, cudaEventRecord(a, c->stream));
-    J3G_CUDA(c, launch_fp64_probe(ptr<double>(c->probe), blocks, threads, iters, c->stream));
+    J3G_LAUNCH(c, launch_fp64_probe(ptr<double>(c->probe), blocks, threads, iters, c->stream));
     J3G_CUDA(c, cudaEventRecord(b, c->stream));
     J3G_CUDA(c, cudaEventSynchronize(b));
     float ms = 0;
