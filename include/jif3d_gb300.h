@@ -36,7 +36,8 @@ enum j3g_status {
   J3G_ERR_CUDA = 2,        /* CUDA runtime error (message in j3g_last_error) */
   J3G_ERR_NOMEM = 3,       /* device or host allocation failed */
   J3G_ERR_STATE = 4,       /* call made before the mesh / stations / kind were set */
-  J3G_ERR_UNSUPPORTED = 5  /* combination not supported (e.g. I2 transform on scalar data) */
+  J3G_ERR_UNSUPPORTED = 5, /* combination not supported (e.g. I2 transform on scalar data) */
+  J3G_ERR_SCRATCH_LIMIT = 6 /* problem too large for j3g_forward_noalloc's fixed scratch */
 };
 
 enum j3g_kind {
@@ -123,6 +124,36 @@ int j3g_lqderivative_device(j3g_context *ctx, const double *d_model, const doubl
 int j3g_synchronize(j3g_context *ctx);
 /* Number of CUDA kernels this context has queued since it was created. */
 int j3g_launch_count(const j3g_context *ctx, long long *count);
+
+/* Allocation-free gridded forward, for callers that cannot let a library
+ * allocate device memory: hosts that reserve all device memory for their own
+ * pool allocator at start-up, or loops that must not take the device-wide
+ * synchronisation of cudaMalloc / cudaFree.  No counterpart in the reference.
+ *
+ * Computes the raw gridded data (no background layers, no transform) of
+ * every station, nmeas * raw values into d_data, for the model d_model
+ * (nx*ny*nz values).  d_xnode / d_ynode / d_znode are the nx+1 / ny+1 / nz+1
+ * mesh node coordinates, i.e. corner coordinates that are the running sums of
+ * the cell sizes (ThreeDModelBase::CalcCoords).  All pointers are device
+ * memory of the current device; work is queued on `stream` (a cudaStream_t,
+ * NULL for the legacy default stream) and the call does not synchronise.
+ *
+ * Scratch is a fixed 16 MiB device array inside the library (held by every
+ * GPU that loads the library until the process exits): the call allocates and
+ * frees nothing.  It needs (nx+1)(ny+1)(nz+1) + 7*nmeas doubles plus at least
+ * one block of nmeas*ncomp doubles (ncomp = 1 scalar, 6 tensor / magnetic,
+ * 7 joint), all rounded up to 32 doubles, within 2^21 doubles; larger problems
+ * return J3G_ERR_SCRATCH_LIMIT without touching d_data.  Every call shares
+ * the array and leaves its last contents behind (each call writes all it
+ * reads, nothing needs to start at zero), so calls that overlap on the GPU
+ * race on it and must be serialised by the caller.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress, with that
+ * device current); make that first call before any stream capture. */
+int j3g_forward_noalloc(int kind, int nx, int ny, int nz, const double *d_xnode,
+                        const double *d_ynode, const double *d_znode, int nmeas,
+                        const double *d_sx, const double *d_sy, const double *d_sz,
+                        double inclination, double declination, double field_strength,
+                        const double *d_model, double *d_data, void *stream);
 
 /* Measured FP64 FMA rate of the device in GFLOP/s (2 flops per FMA), from a
  * dependent-chain probe kernel; used for the FP64 roofline. */

@@ -13,7 +13,7 @@ import numpy as np
 
 from . import build as _build
 
-OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_UNSUPPORTED = range(6)
+OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_UNSUPPORTED, ERR_SCRATCH_LIMIT = range(7)
 SCALAR, TENSOR, MAGNETIC, JOINT = 1, 2, 3, 4
 T_NONE, T_FTG_INVARIANT, T_TOTAL_FIELD, T_TFA = 0, 1, 2, 3
 
@@ -46,6 +46,8 @@ SIGNATURES = {
     "j3g_launch_count": (_I, [_VP, ctypes.POINTER(_LL)]),
     "j3g_probe_fp64": (_I, [_VP, _P]),
     "j3g_probe_math": (_I, [_I, _I]),
+    "j3g_forward_noalloc": (_I, [_I, _I, _I, _I, _VP, _VP, _VP, _I, _VP, _VP, _VP, _D, _D, _D,
+                                 _VP, _VP, _VP]),
 }
 
 _lib = None

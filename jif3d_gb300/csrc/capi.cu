@@ -380,6 +380,7 @@ const char *j3g_status_string(int status) {
     case J3G_ERR_NOMEM: return "out of memory";
     case J3G_ERR_STATE: return "context not ready";
     case J3G_ERR_UNSUPPORTED: return "unsupported combination";
+    case J3G_ERR_SCRATCH_LIMIT: return "problem exceeds the fixed scratch of j3g_forward_noalloc";
     default: return "unknown status";
   }
 }
