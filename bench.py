@@ -1,22 +1,27 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 prism path: Mcell*station/s of forward + adjoint.
 
-Workloads (synthetic, seeded; see jif3d_gb300/workloads.py):
-  plain   -- FP64 matrix-free forward + adjoint (LQDerivative) of one model,
-             box terms recomputed on every call, on the 64x64x32 mesh with
-             32x32 stations, g_z + FTG (joint, 10 raw values per station).
+Workloads (synthetic, seeded; jif3d_gb300/workloads.py):
+  batched (default) -- config 4: 64x64x32 cells (50 m, layers 25 m x1.05),
+      32x32 stations at z = -50 m, joint g_z + FTG, 256 density models
+      (Gaussian blobs + N(0, 0.05) g/cm^3).  The sensitivity is built once per
+      geometry from the FP64 box terms and kept in HBM as fp16 hi + lo with a
+      power-of-two row scale (as FullSensitivityGravMagCalculator keeps J
+      between calls).  A step = batched forward of the 256 models, the weighted misfit
+      (d - d_obs)/sigma^2, and the batched adjoint 2 J^T r, products on the
+      tensor cores.
+  plain -- the FP64 matrix-free forward + adjoint of one model on the same
+      survey (box terms recomputed every call).
 
-A step = one forward and one adjoint over the whole survey.  `value` counts
-cells x stations per second with inputs resident in HBM; `e2e` is the same
-through the public C ABI with host buffers (copies inside the timed region).
-
---impl reference times the CPU oracle (the C restatement of the reference's
-OpenMP implementation, run with all host threads) on a bounded station
-sample of the same workload.
+`value` counts cells x stations x models per second with inputs resident in
+HBM; `e2e` is the same through the C ABI with host buffers (copies inside
+the timed region).  `--impl reference` times the CPU oracle (the C
+restatement of the reference's implementation) on a bounded sample.
 """
 from __future__ import annotations
 
 import argparse
+import concurrent.futures as cf
 import json
 import os
 import statistics
@@ -32,29 +37,28 @@ sys.path.insert(0, ROOT)
 METRIC = "Mcell*station/s fwd+adjoint"
 UNIT = "Mcell*station/s"
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
+SIGMA_GZ, SIGMA_U = 1e-8, 1e-9
 
-# FP64 flop-equivalents per node evaluation of the joint (g_z + 6 FTG) node
-# terms: 21 add/mul + 1 sqrt + 3 ln + 4 atan2 with the per-call weights
-# measured by ncu FP64 instruction counters (sqrt 13, ln 44, atan2 59.5;
-# profiles/fp64_weights.md), plus 7 accumulation FMA.
-FP64_FLOP_PER_NODE = {"joint": 418.0}
+# FP64 flop-equivalents per joint node evaluation: 21 add/mul + sqrt + 3 ln +
+# 4 atan2 + 7 accumulation FMA with the ncu-measured weights sqrt 13, ln 44,
+# atan2 59.5 (profiles/fp64_weights.md).
+FP64_FLOP_PER_JOINT_NODE = 418.0
 
 
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["plain"], default="plain")
+    p.add_argument("--workload", choices=["batched", "plain"], default="batched")
+    p.add_argument("--models", type=int, default=256)
     return p.parse_args()
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
 class ClockSampler:
@@ -81,7 +85,7 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
         out, _ = self.proc.communicate(timeout=10)
-        sm, smax, reasons = [], [], set()
+        sm, smax, power, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in out.strip().splitlines():
             f = [x.strip() for x in line.split(",")]
@@ -90,6 +94,7 @@ class ClockSampler:
             try:
                 sm.append(float(f[1]))
                 smax.append(float(f[2]))
+                power.append(float(f[3]))
             except ValueError:
                 continue
             for n, v in zip(names, f[5:9]):
@@ -97,16 +102,16 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "power_w_max": max(power) if power else None, "samples": len(sm)}
 
 
-def workload(name):
-    from jif3d_gb300 import workloads as W
-    if name == "plain":
-        s = W.config4(nmodels=1)
-        s.models = None
-        return s
-    raise ValueError(name)
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, \
+            "fallback"
 
 
 def barrier(world):
@@ -125,25 +130,194 @@ def max_over_ranks(v, world):
     return float(t.item())
 
 
-def run_ours(args, rank, world, local):
+def sigma_vector(s):
+    n = s.stations.shape[0]
+    return np.tile(np.array([SIGMA_GZ] + [SIGMA_U] * 9), n)
+
+
+def timed_steps(step, nsteps, stream, flush):
+    import torch
+    times = []
+    for _ in range(nsteps):
+        flush.zero_()  # L2 flush between timed steps (outside the events)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step()
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    return times
+
+
+def run_batched(args, rank, world, local):
     import torch
     from jif3d_gb300 import capi, workloads as W
     torch.cuda.set_device(local)
-    s = workload(args.workload)
+    dev = torch.device("cuda", local)
+    s = W.config4(nmodels=args.models)
+    nmod = s.models.shape[0]
     ctx = capi.Context(local)
-    # a dedicated (non-default) stream: the engine and the CUDA events share it
     stream = torch.cuda.Stream(device=local)
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     W.setup_context(ctx, s)
     n = s.stations.shape[0]
-    units = s.ngrid * n  # cells x stations per step
+    R, K = n * 7, s.ngrid
+    units = s.ngrid * n * nmod
+
+    # observed data: FP64 matrix-free response of the base model + noise
+    sig = sigma_vector(s)
+    d_base = torch.tensor(s.model, dtype=torch.float64, device=dev)
+    d_obs = torch.zeros(n * 10, dtype=torch.float64, device=dev)
+    ctx.forward_device(d_base.data_ptr(), d_obs.data_ptr())
+    ctx.synchronize()
+    rng = np.random.default_rng(44)
+    d_obs += torch.tensor(sig * rng.normal(size=n * 10), dtype=torch.float64, device=dev)
+    w = torch.tensor(1.0 / sig ** 2, dtype=torch.float64, device=dev)
+
+    # sensitivity build (once per geometry, outside the timed steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    e1.record(stream)
+    e1.synchronize()
+    build_ms = e0.elapsed_time(e1)
+    info = ctx.sensitivity_info()
+
+    models = torch.tensor(s.models, dtype=torch.float64, device=dev)
+    data = torch.zeros((nmod, n * 10), dtype=torch.float64, device=dev)
+    misfit = torch.zeros_like(data)
+    grads = torch.zeros_like(models)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        ctx.batched_forward_device(nmod, models.data_ptr(), data.data_ptr())
+        torch.mul(torch.sub(data, d_obs, out=misfit), w, out=misfit)
+        ctx.batched_lqderivative_device(nmod, models.data_ptr(), misfit.data_ptr(),
+                                        grads.data_ptr())
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ctx.set_timing(True)
+    l0 = ctx.launch_count()
+    times = timed_steps(step, args.steps, stream, flush)
+    launches = ctx.launch_count() - l0
+    gf_ms, gf_n = ctx.get_timing(capi.TIMER_GEMM_FORWARD)
+    ga_ms, ga_n = ctx.get_timing(capi.TIMER_GEMM_ADJOINT)
+    ctx.set_timing(False)
+    ctx.synchronize()
+    clk = clocks.stop()
+    barrier(world)
+    total_ms = max_over_ranks(sum(times), world)
+    ms_per_step = total_ms / args.steps
+    value = units * world * args.steps / (total_ms * 1e-3) / 1e6
+
+    # accuracy of the mixed path against the FP64 matrix-free path (model 0, 1)
+    errs = {"data_gz": 0.0, "data_ftg": 0.0, "grad": 0.0}
+    for i in (0, nmod - 1):
+        ref = torch.zeros(n * 10, dtype=torch.float64, device=dev)
+        gref = torch.zeros(s.nparm, dtype=torch.float64, device=dev)
+        ctx.forward_device(models[i].data_ptr(), ref.data_ptr())
+        ctx.lqderivative_device(models[i].data_ptr(), misfit[i].data_ptr(), gref.data_ptr())
+        ctx.synchronize()
+        a, r = data[i].view(n, 10), ref.view(n, 10)
+        errs["data_gz"] = max(errs["data_gz"], float(torch.linalg.norm(a[:, 0] - r[:, 0]) /
+                                                     torch.linalg.norm(r[:, 0])))
+        errs["data_ftg"] = max(errs["data_ftg"], float(torch.linalg.norm(a[:, 1:] - r[:, 1:]) /
+                                                       torch.linalg.norm(r[:, 1:])))
+        errs["grad"] = max(errs["grad"], float(torch.linalg.norm(grads[i] - gref) /
+                                               torch.linalg.norm(gref)))
+
+    # plain FP64 matrix-free path, one model, same survey (for the ratio)
+    plain_t = []
+    for it in range(3):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.forward_device(models[0].data_ptr(), data[0].data_ptr())
+        ctx.lqderivative_device(models[0].data_ptr(), misfit[0].data_ptr(), grads[0].data_ptr())
+        b.record(stream)
+        b.synchronize()
+        if it > 0:
+            plain_t.append(a.elapsed_time(b))
+    plain_ms = statistics.median(plain_t)
+    plain_value = s.ngrid * n / (plain_ms * 1e-3) / 1e6
+
+    # end to end through the C ABI with host buffers
+    models_h = np.ascontiguousarray(s.models)
+    obs_h = d_obs.cpu().numpy()
+    w_h = 1.0 / sig ** 2
+    for _ in range(2):
+        dh = ctx.batched_forward(models_h)
+        ctx.batched_lqderivative(models_h, (dh - obs_h) * w_h)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        dh = ctx.batched_forward(models_h)
+        mh = (dh - obs_h) * w_h
+        gh = ctx.batched_lqderivative(models_h, mh)
+    t1 = time.perf_counter()
+    e2e_s = max_over_ranks(t1 - t0, world)
+    e2e = {"value": units * world * args.steps / e2e_s / 1e6, "unit": UNIT,
+           "h2d_bytes_per_step": 8 * (2 * models_h.size + mh.size),
+           "d2h_bytes_per_step": 8 * (dh.size + gh.size)}
+
+    peaks, src = measured_peaks()
+    flops = 3 * 2.0 * R * nmod * K  # per GEMM launch, either direction
+    gemm_ms = (gf_ms + ga_ms) / max(1, gf_n + ga_n)
+    achieved = flops / (gemm_ms * 1e-3) / 1e12
+    j_bytes = 2 * R * info["cols"] * 2  # hi + lo read once per launch
+    # fp16 and bf16 MMA (kind::f16) share one dense rate; the measured cuBLAS
+    # bf16 figure is the denominator
+    roof = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"],
+            "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"], "traffic": None,
+            "peak_source": f"{src} bf16_tflops (burst; fp16 MMA runs at the bf16 rate)",
+            "kernel": "k_gemm_x3<128, fp16> (3 fp16 products per launch)",
+            "ms_per_launch": {"forward": gf_ms / max(1, gf_n), "adjoint": ga_ms / max(1, ga_n)},
+            "hbm_gbs_of_J_stream": j_bytes / (gemm_ms * 1e-3) / 1e9,
+            "hbm_peak_gbs": peaks["hbm_gbs"]}
+    ctx.close()
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp16x2 (hi+lo) J and models, fp32 accum drained per k-block, fp64 sums",
+        "data": "synthetic",
+        "config": {"workload": s.name + "_f16x2_256models", "cells": s.ngrid, "stations": n,
+                   "models": nmod, "rows": R, "kind": "joint g_z + FTG",
+                   "l2": "flushed between timed steps (512 MiB write); J (3.8 GB per direction) "
+                         "exceeds L2",
+                   "sensitivity_build_ms": build_ms, "sensitivity_bytes": info["bytes"],
+                   "parallelism": f"replicas{world}"},
+        "rel_err_vs_fp64": errs,
+        "plain_fp64": {"value": plain_value, "unit": UNIT, "ms_per_step": plain_ms,
+                       "what": "FP64 matrix-free fwd+adjoint of one model, same survey"},
+        "speedup_vs_plain_fp64": value / plain_value,
+        "e2e": e2e, "gpu_launches": launches, "roofline": roof, "clocks": clk,
+    }
+
+
+def run_plain(args, rank, world, local):
+    import torch
+    from jif3d_gb300 import capi, workloads as W
+    torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    s = W.config4(nmodels=1)
+    ctx = capi.Context(local)
+    stream = torch.cuda.Stream(device=local)
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    W.setup_context(ctx, s)
+    n = s.stations.shape[0]
+    units = s.ngrid * n
     d_model = torch.tensor(s.model, dtype=torch.float64, device=dev)
-    d_data = torch.zeros(n * s.dpm, dtype=torch.float64, device=dev)
+    d_data = torch.zeros(n * 10, dtype=torch.float64, device=dev)
     d_grad = torch.zeros(s.nparm, dtype=torch.float64, device=dev)
-    rng = np.random.default_rng(1)
-    misfit_h = rng.normal(size=n * s.dpm)
+    misfit_h = np.random.default_rng(1).normal(size=n * 10)
     d_misfit = torch.tensor(misfit_h, dtype=torch.float64, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
@@ -155,54 +329,36 @@ def run_ours(args, rank, world, local):
         step()
     torch.cuda.synchronize()
     barrier(world)
-    torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
+    ctx.set_timing(True)
     l0 = ctx.launch_count()
-    times = []
-    for _ in range(args.steps):
-        flush.zero_()  # L2 flush between timed steps (outside the events)
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        step()
-        b.record(stream)
-        b.synchronize()
-        times.append(a.elapsed_time(b))
-    torch.cuda.synchronize()
+    times = timed_steps(step, args.steps, stream, flush)
     launches = ctx.launch_count() - l0
+    nf_ms, nf_n = ctx.get_timing(capi.TIMER_NODE_FORWARD)
+    na_ms, na_n = ctx.get_timing(capi.TIMER_NODE_ADJOINT)
+    ctx.set_timing(False)
     clk = clocks.stop()
     barrier(world)
     total_ms = max_over_ranks(sum(times), world)
     ms_per_step = total_ms / args.steps
     value = units * world * args.steps / (total_ms * 1e-3) / 1e6
-
-    # end to end through the C ABI with host buffers (copies in the timed region)
     model_h = s.model.copy()
     for _ in range(2):
         ctx.forward(model_h)
         ctx.lqderivative(model_h, misfit_h)
-    torch.cuda.synchronize()
-    barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        data_h = ctx.forward(model_h)
-        grad_h = ctx.lqderivative(model_h, misfit_h)
-    t1 = time.perf_counter()
-    e2e_s = max_over_ranks(t1 - t0, world)
+        dh = ctx.forward(model_h)
+        gh = ctx.lqderivative(model_h, misfit_h)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e = {"value": units * world * args.steps / e2e_s / 1e6, "unit": UNIT,
            "h2d_bytes_per_step": 8 * (2 * s.nparm + misfit_h.size),
-           "d2h_bytes_per_step": 8 * (data_h.size + grad_h.size)}
-
-    # FP64 roofline of the node kernels
+           "d2h_bytes_per_step": 8 * (dh.size + gh.size)}
     peak = ctx.probe_fp64()
     nodes = (s.shape[0] + 1) * (s.shape[1] + 1) * (s.shape[2] + 1)
-    fpn = FP64_FLOP_PER_NODE["joint"]
-    roof = None
-    if fpn:
-        achieved = 2 * nodes * n * fpn / (ms_per_step * 1e-3) / 1e9
-        roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "GFLOP/s",
-                "frac": achieved / peak, "traffic": None,
-                "peak_source": "measured FP64 FMA probe (MEASURED_PEAKS.json has no FP64 entry)"}
+    node_ms = (nf_ms + na_ms) / max(1, nf_n + na_n)
+    achieved = nodes * n * FP64_FLOP_PER_JOINT_NODE / (node_ms * 1e-3) / 1e9
     ctx.close()
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -211,17 +367,66 @@ def run_ours(args, rank, world, local):
         "config": {"workload": s.name + "_plain_fp64_joint", "cells": s.ngrid, "stations": n,
                    "models": 1, "l2": "flushed between timed steps (512 MiB write)",
                    "parallelism": f"replicas{world}"},
-        "e2e": e2e, "gpu_launches": launches, "roofline": roof, "clocks": clk,
+        "e2e": e2e, "gpu_launches": launches,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "GFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "k_node_forward<JOINT> / k_node_adjoint<JOINT>",
+                     "peak_source": "measured FP64 FMA probe (MEASURED_PEAKS.json has no FP64 "
+                                    "entry)"},
+        "clocks": clk,
     }
 
 
-def cpu_sample_time(s, nthreads, budget_s=12.0):
-    """Time the oracle's forward + LQDerivative on a station sample sized to
-    about budget_s seconds of CPU work; returns (cell*station/s, sample text)."""
+# ---------------------------------------------------------------------------
+# CPU baselines (the oracle: the C restatement of the reference's algorithm)
+
+def cpu_cached_products(budget_s=12.0):
+    """The reference's cached-sensitivity path on the host
+    (FullSensitivityGravMagCalculator: d = J m, g = 2 J^T r per model, FP64),
+    sensitivity rows of a station sample built once, models spread over all
+    host threads.  Returns (cell*station*model/s in M, cores, sample text)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle import oracle as O
+    from helpers import oracle_forward
+    from jif3d_gb300 import workloads as W
+    O.build()
+    s = W.config4()
+    n = s.stations.shape[0]
+    nst = 8
+    sub = s.subset(np.arange(nst) * (n // nst))
+    _, J = oracle_forward(O, sub, want_sens=True)   # 80 x 131072 FP64 rows (not timed)
+    J = np.ascontiguousarray(J)
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(7)
+    r = rng.normal(size=J.shape[0])
+
+    def one(m):
+        O.sens_matvec(J, m)
+        O.sens_rmatvec2(J, r)
+
+    t0 = time.perf_counter()
+    one(s.models[0])
+    t1 = time.perf_counter() - t0
+    nm = int(max(cores, min(s.models.shape[0], budget_s * cores / max(t1, 1e-4))))
+    models = [s.models[i % s.models.shape[0]] for i in range(nm)]
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+        list(ex.map(one, models))
+    t = time.perf_counter() - t0
+    return (s.ngrid * nst * nm / t / 1e6, cores,
+            f"cached-J products (J m and 2 J^T r, FP64) of {nm} models on {nst} of {n} "
+            f"stations x all {s.ngrid} cells, models spread over {cores} threads")
+
+
+def cpu_matrix_free(budget_s=10.0):
+    """The reference's OpenMP matrix-free forward + LQDerivative (one model)
+    on a station sample; all host threads."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from oracle import oracle as O
     from helpers import oracle_forward, oracle_lqderivative
+    from jif3d_gb300 import workloads as W
     O.build()
+    s = W.config4(nmodels=1)
     n = s.stations.shape[0]
 
     def run(k):
@@ -229,31 +434,34 @@ def cpu_sample_time(s, nthreads, budget_s=12.0):
         t0 = time.perf_counter()
         d = oracle_forward(O, sub)
         oracle_lqderivative(O, sub, np.ones(d.size))
-        return time.perf_counter() - t0, sub
+        return time.perf_counter() - t0
 
-    t1, _ = run(1)
+    t1 = run(1)
     k = int(max(1, min(n, budget_s / max(t1, 1e-3))))
-    t, sub = run(k)
-    return s.ngrid * k / t / 1e6, f"{k} of {n} stations x all {s.ngrid} cells, fwd+adjoint"
+    t = run(k)
+    return (s.ngrid * k / t / 1e6, os.cpu_count() or 1,
+            f"OpenMP matrix-free fwd+adjoint, {k} of {n} stations x all {s.ngrid} cells")
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return None
-    s = workload(args.workload)
-    nthreads = os.cpu_count() or 1
-    vals, sample = [], ""
-    for _ in range(max(1, args.steps if args.steps <= 3 else 3)):
-        v, sample = cpu_sample_time(s, nthreads, budget_s=10.0)
+    fn = cpu_cached_products if args.workload == "batched" else cpu_matrix_free
+    vals, cores, sample = [], 1, ""
+    for _ in range(max(1, min(args.steps, 3))):
+        v, cores, sample = fn()
         vals.append(v)
     v = statistics.median(vals)
     return {
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": len(vals),
         "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": s.name + "_plain_fp64_joint", "cells": s.ngrid,
-                   "stations": s.stations.shape[0], "models": 1},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+        "config": {"workload": "config4_batched_64x64x32_" +
+                               ("f16x2_256models" if args.workload == "batched"
+                                else "plain_fp64_joint"),
+                   "cells": 131072, "stations": 1024,
+                   "models": 256 if args.workload == "batched" else 1},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -261,21 +469,24 @@ def run_reference(args, rank, world):
 
 def main():
     args = parse()
-    if args.warmup < 3:
-        args.warmup = 3
+    args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()
     if world > 1:
         import torch.distributed as dist
-        backend = "nccl" if args.impl == "ours" else "gloo"
-        dist.init_process_group(backend=backend)
+        dist.init_process_group(backend="nccl" if args.impl == "ours" else "gloo")
     if args.impl == "reference":
         res = run_reference(args, rank, world)
     else:
-        res = run_ours(args, rank, world, local)
+        run = run_batched if args.workload == "batched" else run_plain
+        res = run(args, rank, world, local)
         if rank == 0:
-            v, sample = cpu_sample_time(workload(args.workload), os.cpu_count() or 1)
-            res["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1,
-                                   "kind": "port", "sample": sample}
+            fn = cpu_cached_products if args.workload == "batched" else cpu_matrix_free
+            v, cores, sample = fn()
+            res["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                   "sample": sample}
+            if args.workload == "batched":
+                v2, _, sample2 = cpu_matrix_free()
+                res["cpu_baseline_matrix_free"] = {"value": v2, "unit": UNIT, "sample": sample2}
     if rank == 0 and res is not None:
         print(json.dumps(res))
     if world > 1:

@@ -120,10 +120,71 @@ int j3g_forward_device(j3g_context *ctx, const double *d_model, double *d_data);
 int j3g_lqderivative_device(j3g_context *ctx, const double *d_model, const double *d_misfit,
                             double *d_grad);
 
-/* Block until the context's stream is idle. */
+/* ---- Device-resident sensitivity matrix ------------------------------------
+ * The GPU counterpart of FullSensitivityGravMagCalculator's cached path
+ * (GravMag/FullSensitivityGravMagCalculator.h:116-221): J is built once per
+ * geometry from the FP64 box terms and kept in HBM; later products reuse it
+ * without recomputing any box term.  Stored rows per station: scalar 1 (g_z),
+ * tensor 6 (Uxx Uyy Uzz Uxy Uxz Uyz), joint 7 (g_z + the 6), magnetic 3
+ * (Bx By Bz); the background columns stay FP64.  Any set_mesh / set_stations
+ * / set_kind / set_background call drops it.  Needs corner coordinates that
+ * are running sums of the cell sizes (as jif3D builds them). */
+enum j3g_storage {
+  J3G_STORE_FP32 = 1, /* FP32 J, streamed by FP32-FMA products with FP64 sums */
+  J3G_STORE_F16X2 = 2 /* J = s_r (hi + lo), fp16 hi / lo (22 significant bits) with a
+                         power-of-two row scale s_r, plus the transposed copy; products on
+                         the tensor cores.  (A bf16 hi / lo pair keeps only 16 bits, which
+                         leaves ~2e-6 relative error on FTG rows.) */
+};
+int j3g_build_sensitivity(j3g_context *ctx, int storage);
+int j3g_drop_sensitivity(j3g_context *ctx);
+/* storage kind, stored rows, columns (cells) and device bytes of the stored J. */
+int j3g_sensitivity_info(const j3g_context *ctx, int *storage, long long *rows, long long *cols,
+                         long long *bytes);
+/* Cached forward d = T(J m) and derivative 2 J^T (T' misfit) of one model
+ * with the stored J (FullSensitivityGravMagCalculator::CalculateCachedResult
+ * :154-167 and CachedLQDerivative :169-221). */
+int j3g_stored_forward_device(j3g_context *ctx, const double *d_model, double *d_data);
+int j3g_stored_lqderivative_device(j3g_context *ctx, const double *d_model,
+                                   const double *d_misfit, double *d_grad);
+/* The same for nmodels models at once (line-search trials, Monte-Carlo
+ * samples): models [nmodels][nparm], data [nmodels][nmeas*data_per_meas],
+ * misfits like data, gradients like models.  With J3G_STORE_F16X2 storage
+ * the products run on the tensor cores: models and scaled misfits are split
+ * into fp16 hi / lo parts with power-of-two scales, J M ~= Jhi Mhi + Jhi Mlo
+ * + Jlo Mhi; the hi*hi products of each 64-wide k-block are drained from TMEM
+ * into FP32 register sums, the cross terms accumulate per K split of at most
+ * 4096 cells, and the splits are summed in FP64 (about 1e-7 relative error).  The _device forms queue work only; the host forms copy
+ * in and out and synchronise. */
+int j3g_batched_forward_device(j3g_context *ctx, int nmodels, const double *d_models,
+                               double *d_data);
+int j3g_batched_lqderivative_device(j3g_context *ctx, int nmodels, const double *d_models,
+                                    const double *d_misfits, double *d_grads);
+int j3g_batched_forward(j3g_context *ctx, int nmodels, const double *h_models, double *h_data);
+int j3g_batched_lqderivative(j3g_context *ctx, int nmodels, const double *h_models,
+                             const double *h_misfits, double *h_grads);
+
+/* Block until the context's stream is idle; reports J3G_ERR_CUDA if a
+ * bounded wait inside a tensor-core kernel expired since the last check. */
 int j3g_synchronize(j3g_context *ctx);
 /* Number of CUDA kernels this context has queued since it was created. */
 int j3g_launch_count(const j3g_context *ctx, long long *count);
+
+/* Kernel timing (for rooflines): while enabled, the dominant launches of each
+ * category are bracketed by CUDA events on the context's stream.
+ * j3g_set_timing(ctx, 1) starts a new measurement (clears old records);
+ * j3g_get_timing synchronises and returns the summed device time (ms) and
+ * the number of timed launches of one category. */
+enum j3g_timer {
+  J3G_TIMER_NODE_FORWARD = 0,   /* k_node_forward */
+  J3G_TIMER_NODE_ADJOINT = 1,   /* k_node_adjoint */
+  J3G_TIMER_STREAM_FORWARD = 2, /* FP32 J m streaming product */
+  J3G_TIMER_STREAM_ADJOINT = 3, /* FP32 J^T r streaming product (column blocks) */
+  J3G_TIMER_GEMM_FORWARD = 4,   /* tensor-core J M */
+  J3G_TIMER_GEMM_ADJOINT = 5    /* tensor-core J^T R */
+};
+int j3g_set_timing(j3g_context *ctx, int enable);
+int j3g_get_timing(j3g_context *ctx, int category, double *total_ms, long long *launches);
 
 /* Allocation-free gridded forward, for callers that cannot let a library
  * allocate device memory: hosts that reserve all device memory for their own

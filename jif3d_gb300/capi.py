@@ -16,6 +16,9 @@ from . import build as _build
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_UNSUPPORTED, ERR_SCRATCH_LIMIT = range(7)
 SCALAR, TENSOR, MAGNETIC, JOINT = 1, 2, 3, 4
 T_NONE, T_FTG_INVARIANT, T_TOTAL_FIELD, T_TFA = 0, 1, 2, 3
+STORE_FP32, STORE_F16X2 = 1, 2
+(TIMER_NODE_FORWARD, TIMER_NODE_ADJOINT, TIMER_STREAM_FORWARD, TIMER_STREAM_ADJOINT,
+ TIMER_GEMM_FORWARD, TIMER_GEMM_ADJOINT) = range(6)
 
 _P = ctypes.POINTER(ctypes.c_double)
 _VP = ctypes.c_void_p
@@ -43,7 +46,19 @@ SIGNATURES = {
     "j3g_forward_device": (_I, [_VP, _VP, _VP]),
     "j3g_lqderivative_device": (_I, [_VP, _VP, _VP, _VP]),
     "j3g_synchronize": (_I, [_VP]),
+    "j3g_build_sensitivity": (_I, [_VP, _I]),
+    "j3g_drop_sensitivity": (_I, [_VP]),
+    "j3g_sensitivity_info": (_I, [_VP, ctypes.POINTER(_I), ctypes.POINTER(_LL),
+                                  ctypes.POINTER(_LL), ctypes.POINTER(_LL)]),
+    "j3g_stored_forward_device": (_I, [_VP, _VP, _VP]),
+    "j3g_stored_lqderivative_device": (_I, [_VP, _VP, _VP, _VP]),
+    "j3g_batched_forward_device": (_I, [_VP, _I, _VP, _VP]),
+    "j3g_batched_lqderivative_device": (_I, [_VP, _I, _VP, _VP, _VP]),
+    "j3g_batched_forward": (_I, [_VP, _I, _P, _P]),
+    "j3g_batched_lqderivative": (_I, [_VP, _I, _P, _P, _P]),
     "j3g_launch_count": (_I, [_VP, ctypes.POINTER(_LL)]),
+    "j3g_set_timing": (_I, [_VP, _I]),
+    "j3g_get_timing": (_I, [_VP, _I, _P, ctypes.POINTER(_LL)]),
     "j3g_probe_fp64": (_I, [_VP, _P]),
     "j3g_probe_math": (_I, [_I, _I]),
     "j3g_forward_noalloc": (_I, [_I, _I, _I, _I, _VP, _VP, _VP, _I, _VP, _VP, _VP, _D, _D, _D,
@@ -196,6 +211,60 @@ class Context:
 
     def synchronize(self):
         self._check(self._lib.j3g_synchronize(self._h))
+
+    # -- device-resident sensitivity ----------------------------------------
+    def build_sensitivity(self, storage):
+        self._check(self._lib.j3g_build_sensitivity(self._h, int(storage)))
+
+    def drop_sensitivity(self):
+        self._check(self._lib.j3g_drop_sensitivity(self._h))
+
+    def sensitivity_info(self):
+        st, r, c, b = _I(), _LL(), _LL(), _LL()
+        self._check(self._lib.j3g_sensitivity_info(self._h, ctypes.byref(st), ctypes.byref(r),
+                                                   ctypes.byref(c), ctypes.byref(b)))
+        return dict(storage=st.value, rows=r.value, cols=c.value, bytes=b.value)
+
+    def stored_forward_device(self, d_model, d_data):
+        self._check(self._lib.j3g_stored_forward_device(self._h, _VP(d_model), _VP(d_data)))
+
+    def stored_lqderivative_device(self, d_model, d_misfit, d_grad):
+        self._check(self._lib.j3g_stored_lqderivative_device(self._h, _VP(d_model),
+                                                             _VP(d_misfit), _VP(d_grad)))
+
+    def batched_forward_device(self, nmodels, d_models, d_data):
+        self._check(self._lib.j3g_batched_forward_device(self._h, int(nmodels), _VP(d_models),
+                                                         _VP(d_data)))
+
+    def batched_lqderivative_device(self, nmodels, d_models, d_misfits, d_grads):
+        self._check(self._lib.j3g_batched_lqderivative_device(self._h, int(nmodels),
+                                                              _VP(d_models), _VP(d_misfits),
+                                                              _VP(d_grads)))
+
+    def batched_forward(self, models):
+        s = self.sizes()
+        m = _f64(models).reshape(-1, s["nparm"])
+        d = np.zeros((m.shape[0], s["nmeas"] * s["dpm"]))
+        self._check(self._lib.j3g_batched_forward(self._h, m.shape[0], _ptr(m), _ptr(d)))
+        return d
+
+    def batched_lqderivative(self, models, misfits):
+        s = self.sizes()
+        m = _f64(models).reshape(-1, s["nparm"])
+        r = _f64(misfits).reshape(m.shape[0], s["nmeas"] * s["dpm"])
+        g = np.zeros_like(m)
+        self._check(self._lib.j3g_batched_lqderivative(self._h, m.shape[0], _ptr(m), _ptr(r),
+                                                       _ptr(g)))
+        return g
+
+    def set_timing(self, enable=True):
+        self._check(self._lib.j3g_set_timing(self._h, 1 if enable else 0))
+
+    def get_timing(self, category):
+        ms, n = _D(), _LL()
+        self._check(self._lib.j3g_get_timing(self._h, int(category), ctypes.byref(ms),
+                                             ctypes.byref(n)))
+        return ms.value, n.value
 
     def launch_count(self):
         v = _LL()

@@ -18,6 +18,7 @@
 
 #include "../../include/jif3d_gb300.h"
 #include "prism_kernels.h"
+#include "stored.h"
 
 using namespace j3g;
 
@@ -58,6 +59,19 @@ struct j3g_context {
   DevBuf model, data, misfit, grad, rhot, partial, comps, bgsens, rawd, wraw, W, Gpart, G, F,
       rows, rowsum, probe;
 
+  // device-resident sensitivity (j3g_build_sensitivity)
+  int storage = 0;             // 0 none, J3G_STORE_FP32, J3G_STORE_F16X2
+  long long st_rows = 0;       // nmeas * stored rows per station
+  long long st_ld = 0;         // cells padded to a multiple of 64
+  long long st_ldT = 0;        // rows padded to a multiple of 64 (transposed copy)
+  DevBuf J32, Jhi, Jlo, JThi, JTlo, rowscale, Jrowsum;
+  DevBuf x32, sums, part, Bhi, Blo, P, wst, wrawb, rawb, gerr, mscale, mmean, swork;
+
+  // optional per-category kernel timing (j3g_set_timing): event pairs
+  // recorded on the context's stream around the dominant launches
+  bool timing = false;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> timed;
+
   long long ngrid() const { return (long long)nx * ny * nz; }
   long long nparm() const { return ngrid() + (long long)bg.size(); }
   long long nnodes() const { return (long long)(nx + 1) * (ny + 1) * (nz + 1); }
@@ -90,6 +104,27 @@ int cuda_fail(j3g_context *c, cudaError_t e, const char *where) {
     if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
     ++(ctx)->launches;                                      \
   } while (0)
+
+// Records a start event now and a stop event when it goes out of scope, if
+// the context's timing is on.
+struct TimedScope {
+  j3g_context *c;
+  int cat;
+  cudaEvent_t a = nullptr, b = nullptr;
+  TimedScope(j3g_context *ctx, int category) : c(ctx), cat(category) {
+    if (!c->timing) return;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+      a = b = nullptr;
+      return;
+    }
+    cudaEventRecord(a, c->stream);
+  }
+  ~TimedScope() {
+    if (!a) return;
+    cudaEventRecord(b, c->stream);
+    c->timed.push_back({cat, {a, b}});
+  }
+};
 
 int ensure(j3g_context *c, DevBuf &b, size_t bytes) {
   if (bytes == 0) bytes = 8;
@@ -212,8 +247,11 @@ int gridded_node_forward(j3g_context *c, const double *d_model) {
   const int ncomp = kind_ncomp(c->kind);
   J3G_TRY(ensure(c, c->partial, sizeof(double) * (size_t)nblk * c->nmeas * ncomp));
   J3G_TRY(ensure(c, c->comps, sizeof(double) * (size_t)c->nmeas * NC_COUNT));
-  J3G_LAUNCH(c, launch_node_forward(c->kind, m, station_view(c), ptr<double>(c->rhot),
-                                  ptr<double>(c->partial), nblk, npb, spb, c->stream));
+  {
+    TimedScope ts(c, J3G_TIMER_NODE_FORWARD);
+    J3G_LAUNCH(c, launch_node_forward(c->kind, m, station_view(c), ptr<double>(c->rhot),
+                                      ptr<double>(c->partial), nblk, npb, spb, c->stream));
+  }
   J3G_LAUNCH(c, launch_forward_reduce(c->kind, c->nmeas, nblk, ptr<double>(c->partial),
                                     ptr<double>(c->comps), c->stream));
   return J3G_OK;
@@ -339,8 +377,11 @@ int adjoint_device(j3g_context *c, const double *d_model, const double *d_misfit
     nchunk = (c->nmeas + spc - 1) / spc;
     J3G_TRY(ensure(c, c->Gpart, sizeof(double) * (size_t)nchunk * nn));
     J3G_TRY(ensure(c, c->G, sizeof(double) * (size_t)nn));
-    J3G_LAUNCH(c, launch_node_adjoint(c->kind, m, s, ptr<double>(c->W), spc, nchunk,
-                                    ptr<double>(c->Gpart), c->stream));
+    {
+      TimedScope ts(c, J3G_TIMER_NODE_ADJOINT);
+      J3G_LAUNCH(c, launch_node_adjoint(c->kind, m, s, ptr<double>(c->W), spc, nchunk,
+                                        ptr<double>(c->Gpart), c->stream));
+    }
     J3G_LAUNCH(c, launch_adjoint_combine(m, nchunk, ptr<double>(c->Gpart), ptr<double>(c->G),
                                        d_grad, c->stream));
     ++c->launches;  // chunk sum + cell combine
@@ -366,6 +407,293 @@ int adjoint_device(j3g_context *c, const double *d_model, const double *d_misfit
 }
 
 bool valid_kind(int k) { return k >= J3G_SCALAR && k <= J3G_JOINT; }
+
+// ---------------------------------------------------------------------------
+// Device-resident sensitivity (the GPU side of FullSensitivityGravMagCalculator)
+
+void free_buf(DevBuf &b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+}
+
+void drop_stored(j3g_context *c) {
+  if (!c || c->storage == 0) return;
+  cudaStreamSynchronize(c->stream);
+  free_buf(c->J32);
+  free_buf(c->Jhi);
+  free_buf(c->Jlo);
+  free_buf(c->JThi);
+  free_buf(c->JTlo);
+  free_buf(c->rowscale);
+  free_buf(c->Jrowsum);
+  c->storage = 0;
+}
+
+long long round64(long long v) { return (v + 63) / 64 * 64; }
+int nstored(const j3g_context *c) { return stored_rows_per_station(c->kind); }
+
+int build_stored(j3g_context *c, int storage) {
+  J3G_TRY(check_ready(c));
+  if (storage != J3G_STORE_FP32 && storage != J3G_STORE_F16X2)
+    return fail(c, J3G_ERR_ARG, "unknown storage");
+  if (!c->node_exact)
+    return fail(c, J3G_ERR_UNSUPPORTED,
+                "device sensitivity needs corner coordinates that are running sums of the sizes");
+  if (c->ngrid() == 0 || c->nmeas == 0) return fail(c, J3G_ERR_ARG, "empty mesh or survey");
+  drop_stored(c);
+  J3G_TRY(ensure_background(c));
+  const long long K = c->ngrid(), ldK = round64(K);
+  const int NS = nstored(c);
+  const long long R = (long long)c->nmeas * NS, ldR = round64(R);
+  const size_t need = storage == J3G_STORE_FP32 ? (size_t)R * ldK * 4 : (size_t)(R * ldK + K * ldR) * 4;
+  size_t fr = 0, tot = 0;
+  J3G_CUDA(c, cudaMemGetInfo(&fr, &tot));
+  if (need + (size_t)(1ull << 31) > fr)
+    return fail(c, J3G_ERR_NOMEM, "sensitivity of " + std::to_string(need) + " bytes does not fit");
+  c->st_rows = R;
+  c->st_ld = ldK;
+  c->st_ldT = ldR;
+  // station chunks bounded by ~1 GiB of FP64 rows + node scratch
+  const long long per = (long long)NS * K * 8 + (long long)kind_ncomp(c->kind) * c->nnodes() * 8;
+  int chunk = (int)std::max(1LL, std::min<long long>(c->nmeas, (1LL << 30) / per));
+  chunk = std::min(chunk, 65535);
+  J3G_TRY(ensure(c, c->F, sizeof(double) * (size_t)chunk * kind_ncomp(c->kind) * c->nnodes()));
+  MeshView m = mesh_view(c);
+  StationView s = station_view(c);
+  const MagField mf = mag_field(c);
+  if (storage == J3G_STORE_FP32) {
+    J3G_TRY(ensure(c, c->J32, sizeof(float) * (size_t)R * ldK));
+    J3G_CUDA(c, cudaMemsetAsync(c->J32.p, 0, sizeof(float) * (size_t)R * ldK, c->stream));
+    for (int s0 = 0; s0 < c->nmeas; s0 += chunk) {
+      const int ns = std::min(chunk, c->nmeas - s0);
+      J3G_LAUNCH(c, launch_stored_rows(c->kind, m, s, s0, ns, mf, ptr<double>(c->F), nullptr,
+                                       ptr<float>(c->J32) + (size_t)s0 * NS * ldK, ldK,
+                                       c->stream));
+      ++c->launches;
+    }
+  } else {
+    J3G_TRY(ensure(c, c->Jhi, 2 * (size_t)R * ldK));
+    J3G_TRY(ensure(c, c->Jlo, 2 * (size_t)R * ldK));
+    J3G_TRY(ensure(c, c->JThi, 2 * (size_t)K * ldR));
+    J3G_TRY(ensure(c, c->JTlo, 2 * (size_t)K * ldR));
+    J3G_TRY(ensure(c, c->rowscale, sizeof(float) * (size_t)R));
+    J3G_TRY(ensure(c, c->Jrowsum, sizeof(double) * (size_t)R));
+    J3G_TRY(ensure(c, c->rows, sizeof(double) * (size_t)chunk * NS * K));
+    J3G_TRY(ensure(c, c->gerr, sizeof(int)));
+    J3G_CUDA(c, cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream));
+    for (int s0 = 0; s0 < c->nmeas; s0 += chunk) {
+      const int ns = std::min(chunk, c->nmeas - s0);
+      J3G_LAUNCH(c, launch_stored_rows(c->kind, m, s, s0, ns, mf, ptr<double>(c->F),
+                                       ptr<double>(c->rows), nullptr, K, c->stream));
+      ++c->launches;
+      J3G_LAUNCH(c, launch_split_rows(ptr<double>(c->rows), K, K, ns * NS, c->Jhi.p, c->Jlo.p,
+                                      ldK, ptr<float>(c->rowscale), ptr<double>(c->Jrowsum),
+                                      (long long)s0 * NS, c->stream));
+    }
+    J3G_LAUNCH(c, launch_transpose16(c->Jhi.p, ldK, R, K, c->JThi.p, ldR, c->stream));
+    J3G_LAUNCH(c, launch_transpose16(c->Jlo.p, ldK, R, K, c->JTlo.p, ldR, c->stream));
+  }
+  J3G_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->storage = storage;
+  return J3G_OK;
+}
+
+int check_stored(j3g_context *c) {
+  J3G_TRY(check_ready(c));
+  if (c->storage == 0) return fail(c, J3G_ERR_STATE, "no device sensitivity: call j3g_build_sensitivity");
+  return J3G_OK;
+}
+
+int batched_forward_impl(j3g_context *c, int nmod, const double *d_models, double *d_data,
+                         double *raw_out);
+
+// d = J m through the FP32 streaming product (one model), then background + transform.
+int stored_forward_f32(j3g_context *c, const double *d_model, double *d_data, double *raw_out) {
+  const long long K = c->ngrid(), ldK = c->st_ld, R = c->st_rows;
+  double tbx, tby, tbz;
+  tfa_dir(c, tbx, tby, tbz);
+  J3G_TRY(ensure(c, c->x32, sizeof(float) * (size_t)ldK));
+  J3G_TRY(ensure(c, c->sums, sizeof(double) * (size_t)R));
+  J3G_LAUNCH(c, launch_to_f32(d_model, K, ldK, ptr<float>(c->x32), c->stream));
+  {
+    TimedScope ts(c, J3G_TIMER_STREAM_FORWARD);
+    J3G_LAUNCH(c, launch_gemv_f32(ptr<float>(c->J32), ldK, (int)R, ptr<float>(c->x32),
+                                  ptr<double>(c->sums), c->stream));
+  }
+  const int nbg = (int)c->bg.size();
+  J3G_LAUNCH(c, launch_stored_assemble(c->kind, c->transform, tbx, tby, tbz, c->nmeas, 1,
+                                       ptr<double>(c->sums), R, nbg ? ptr<double>(c->bgsens) : nullptr,
+                                       nbg, d_model, c->nparm(), K, mag_field(c), raw_out, d_data,
+                                       (long long)c->nmeas * c->dpm(), c->stream));
+  return J3G_OK;
+}
+
+int stored_adjoint_f32(j3g_context *c, const double *d_model, const double *d_misfit,
+                       double *d_grad) {
+  const long long K = c->ngrid(), ldK = c->st_ld, R = c->st_rows;
+  const int raw = c->raw(), nbg = (int)c->bg.size();
+  double tbx, tby, tbz;
+  tfa_dir(c, tbx, tby, tbz);
+  const double *rawd = nullptr;
+  if (c->transform == J3G_T_FTG_INVARIANT || c->transform == J3G_T_TOTAL_FIELD) {
+    J3G_TRY(ensure(c, c->rawb, sizeof(double) * (size_t)c->nmeas * raw));
+    J3G_TRY(ensure(c, c->data, sizeof(double) * (size_t)c->nmeas * c->dpm()));
+    J3G_TRY(stored_forward_f32(c, d_model, ptr<double>(c->data), ptr<double>(c->rawb)));
+    rawd = ptr<double>(c->rawb);
+  }
+  J3G_TRY(ensure(c, c->wrawb, sizeof(double) * (size_t)c->nmeas * raw));
+  J3G_TRY(ensure(c, c->wst, sizeof(double) * (size_t)R));
+  J3G_TRY(ensure(c, c->part, sizeof(double) * (size_t)gemv_t_chunks((int)R) * ldK));
+  J3G_LAUNCH(c, launch_stored_weights(c->kind, c->transform, tbx, tby, tbz, c->nmeas, 1, d_misfit,
+                                      (long long)c->nmeas * c->dpm(), rawd, mag_field(c),
+                                      ptr<double>(c->wrawb), ptr<double>(c->wst), R, c->stream));
+  {
+    TimedScope ts(c, J3G_TIMER_STREAM_ADJOINT);
+    J3G_LAUNCH(c, launch_gemv_t_f32(ptr<float>(c->J32), ldK, (int)R, ptr<double>(c->wst),
+                                    ptr<double>(c->part), K, 2.0, d_grad, c->stream));
+  }
+  ++c->launches;  // column-block sums + chunk reduction
+  if (nbg)
+    J3G_LAUNCH(c, launch_bg_grad_batched(raw, c->nmeas, nbg, 1, ptr<double>(c->wrawb),
+                                         ptr<double>(c->bgsens), d_grad, c->nparm(), K, c->stream));
+  return J3G_OK;
+}
+
+// K-splits of a tensor-core product: at most 64 k-blocks (4096 products) per
+// split keep the kernel's FP32 register sums short (the splits are added in
+// FP64), and at least about six waves of CTAs over the 152 SMs.
+int choose_splits(long long m, int ntiles, long long ld) {
+  const long long mt = (m + 127) / 128, kb = ld / 64;
+  const long long s = std::max<long long>((kb + 63) / 64,
+                                          (6 * 152 + mt * ntiles - 1) / (mt * ntiles));
+  return (int)std::max<long long>(1, std::min(s, kb));
+}
+
+int batched_forward_impl(j3g_context *c, int nmod, const double *d_models, double *d_data,
+                         double *raw_out) {
+  const long long K = c->ngrid(), ldK = c->st_ld, R = c->st_rows, np = c->nparm();
+  double tbx, tby, tbz;
+  tfa_dir(c, tbx, tby, tbz);
+  const int nbg = (int)c->bg.size();
+  J3G_TRY(ensure(c, c->sums, sizeof(double) * (size_t)nmod * R));
+  if (c->storage == J3G_STORE_FP32) {
+    for (int n = 0; n < nmod; ++n) {
+      J3G_TRY(ensure(c, c->x32, sizeof(float) * (size_t)ldK));
+      J3G_LAUNCH(c, launch_to_f32(d_models + (size_t)n * np, K, ldK, ptr<float>(c->x32), c->stream));
+      J3G_LAUNCH(c, launch_gemv_f32(ptr<float>(c->J32), ldK, (int)R, ptr<float>(c->x32),
+                                    ptr<double>(c->sums) + (size_t)n * R, c->stream));
+    }
+  } else {
+    const int tile = gemm_n_tile(nmod);
+    const long long npad = (nmod + tile - 1) / tile * tile;
+    J3G_TRY(ensure(c, c->Bhi, 2 * (size_t)npad * ldK));
+    J3G_TRY(ensure(c, c->Blo, 2 * (size_t)npad * ldK));
+    J3G_TRY(ensure(c, c->mscale, sizeof(float) * (size_t)npad));
+    J3G_TRY(ensure(c, c->mmean, sizeof(double) * (size_t)npad));
+    J3G_TRY(ensure(c, c->swork, sizeof(double) * (size_t)split_matrix_work((int)npad, ldK)));
+    // models are centred (m - mean over cells); mean * (J 1) is added back in
+    // FP64 after the product, so a large uniform part of a model -- whose
+    // tensor response is nearly zero -- does not eat into the FP32 accuracy
+    J3G_LAUNCH(c, launch_split_matrix(d_models, np, nmod, K, nullptr, c->Bhi.p, c->Blo.p, ldK,
+                                      (int)npad, ptr<float>(c->mscale), ptr<double>(c->mmean),
+                                      ptr<double>(c->swork), c->stream));
+    c->launches += 2;  // statistics, finalise and split passes
+    const int nsplit = choose_splits(R, (int)(npad / tile), ldK);
+    const int nsp = gemm_splits_used(ldK, nsplit);
+    const long long slice = (long long)nmod * R;
+    J3G_TRY(ensure(c, c->P, sizeof(float) * (size_t)nsp * slice));
+    J3G_TRY(ensure(c, c->gerr, sizeof(int)));
+    GemmOperands g{c->Jhi.p, c->Jlo.p, R, c->Bhi.p, c->Blo.p, nmod, npad, ldK, true};
+    {
+      TimedScope ts(c, J3G_TIMER_GEMM_FORWARD);
+      J3G_LAUNCH(c, launch_gemm_x3(g, nsplit, ptr<float>(c->P), R, slice, ptr<int>(c->gerr),
+                                   c->stream));
+    }
+    J3G_LAUNCH(c, launch_splitk_reduce(ptr<float>(c->P), nsp, slice, nmod, (int)R, R,
+                                       ptr<float>(c->rowscale), ptr<float>(c->mscale),
+                                       ptr<double>(c->mmean), ptr<double>(c->Jrowsum), 1.0,
+                                       ptr<double>(c->sums), R, c->stream));
+  }
+  J3G_LAUNCH(c, launch_stored_assemble(c->kind, c->transform, tbx, tby, tbz, c->nmeas, nmod,
+                                       ptr<double>(c->sums), R, nbg ? ptr<double>(c->bgsens) : nullptr,
+                                       nbg, d_models, np, K, mag_field(c), raw_out, d_data,
+                                       (long long)c->nmeas * c->dpm(), c->stream));
+  return J3G_OK;
+}
+
+int batched_adjoint_impl(j3g_context *c, int nmod, const double *d_models,
+                         const double *d_misfits, double *d_grads) {
+  const long long K = c->ngrid(), ldK = c->st_ld, R = c->st_rows, ldR = c->st_ldT,
+                  np = c->nparm();
+  const int raw = c->raw(), nbg = (int)c->bg.size();
+  double tbx, tby, tbz;
+  tfa_dir(c, tbx, tby, tbz);
+  const double *rawd = nullptr;
+  if (c->transform == J3G_T_FTG_INVARIANT || c->transform == J3G_T_TOTAL_FIELD) {
+    J3G_TRY(ensure(c, c->rawb, sizeof(double) * (size_t)nmod * c->nmeas * raw));
+    J3G_TRY(ensure(c, c->data, sizeof(double) * (size_t)nmod * c->nmeas * c->dpm()));
+    J3G_TRY(batched_forward_impl(c, nmod, d_models, ptr<double>(c->data), ptr<double>(c->rawb)));
+    rawd = ptr<double>(c->rawb);
+  }
+  J3G_TRY(ensure(c, c->wrawb, sizeof(double) * (size_t)nmod * c->nmeas * raw));
+  J3G_TRY(ensure(c, c->wst, sizeof(double) * (size_t)nmod * R));
+  J3G_LAUNCH(c, launch_stored_weights(c->kind, c->transform, tbx, tby, tbz, c->nmeas, nmod,
+                                      d_misfits, (long long)c->nmeas * c->dpm(), rawd, mag_field(c),
+                                      ptr<double>(c->wrawb), ptr<double>(c->wst), R, c->stream));
+  if (c->storage == J3G_STORE_FP32) {
+    J3G_TRY(ensure(c, c->part, sizeof(double) * (size_t)gemv_t_chunks((int)R) * ldK));
+    for (int n = 0; n < nmod; ++n) {
+      J3G_LAUNCH(c, launch_gemv_t_f32(ptr<float>(c->J32), ldK, (int)R,
+                                      ptr<double>(c->wst) + (size_t)n * R, ptr<double>(c->part), K,
+                                      2.0, d_grads + (size_t)n * np, c->stream));
+      ++c->launches;
+    }
+  } else {
+    const int tile = gemm_n_tile(nmod);
+    const long long npad = (nmod + tile - 1) / tile * tile;
+    J3G_TRY(ensure(c, c->Bhi, 2 * (size_t)npad * std::max(ldR, ldK)));
+    J3G_TRY(ensure(c, c->Blo, 2 * (size_t)npad * std::max(ldR, ldK)));
+    J3G_TRY(ensure(c, c->mscale, sizeof(float) * (size_t)npad));
+    J3G_TRY(ensure(c, c->swork, sizeof(double) * (size_t)split_matrix_work((int)npad, ldR)));
+    // residual weights carry the row scale of J: J = s_r (hi + lo)
+    J3G_LAUNCH(c, launch_split_matrix(ptr<double>(c->wst), R, nmod, R, ptr<float>(c->rowscale),
+                                      c->Bhi.p, c->Blo.p, ldR, (int)npad, ptr<float>(c->mscale),
+                                      nullptr, ptr<double>(c->swork), c->stream));
+    c->launches += 2;  // statistics, finalise and split passes
+    const int nsplit = choose_splits(K, (int)(npad / tile), ldR);
+    const int nsp = gemm_splits_used(ldR, nsplit);
+    const long long slice = (long long)nmod * K;
+    J3G_TRY(ensure(c, c->P, sizeof(float) * (size_t)nsp * slice));
+    J3G_TRY(ensure(c, c->gerr, sizeof(int)));
+    GemmOperands g{c->JThi.p, c->JTlo.p, K, c->Bhi.p, c->Blo.p, nmod, npad, ldR, true};
+    {
+      TimedScope ts(c, J3G_TIMER_GEMM_ADJOINT);
+      J3G_LAUNCH(c, launch_gemm_x3(g, nsplit, ptr<float>(c->P), K, slice, ptr<int>(c->gerr),
+                                   c->stream));
+    }
+    J3G_LAUNCH(c, launch_splitk_reduce(ptr<float>(c->P), nsp, slice, nmod, (int)K, K, nullptr,
+                                       ptr<float>(c->mscale), nullptr, nullptr, 2.0, d_grads, np,
+                                       c->stream));
+  }
+  if (nbg)
+    J3G_LAUNCH(c, launch_bg_grad_batched(raw, c->nmeas, nbg, nmod, ptr<double>(c->wrawb),
+                                         ptr<double>(c->bgsens), d_grads, np, K, c->stream));
+  return J3G_OK;
+}
+
+// Error flag of the tensor-core pipeline (bounded waits that expired).
+int check_gemm_flag(j3g_context *c) {
+  if (!c->gerr.p) return J3G_OK;
+  int v = 0;
+  J3G_CUDA(c, cudaMemcpyAsync(&v, c->gerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  J3G_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (v != 0) {
+    cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream);
+    return fail(c, J3G_ERR_CUDA, "tensor-core pipeline wait expired (code " + std::to_string(v) + ")");
+  }
+  return J3G_OK;
+}
 
 }  // namespace
 
@@ -418,9 +746,16 @@ int j3g_destroy(j3g_context *c) {
   DevBuf *bufs[] = {&c->dX, &c->dY, &c->dZ, &c->dxs, &c->dys, &c->dzs, &c->dbg, &c->dsx,
                     &c->dsy, &c->dsz, &c->model, &c->data, &c->misfit, &c->grad, &c->rhot,
                     &c->partial, &c->comps, &c->bgsens, &c->rawd, &c->wraw, &c->W, &c->Gpart,
-                    &c->G, &c->F, &c->rows, &c->rowsum, &c->probe};
+                    &c->G, &c->F, &c->rows, &c->rowsum, &c->probe, &c->J32, &c->Jhi,
+                    &c->Jlo, &c->JThi, &c->JTlo, &c->rowscale, &c->x32, &c->sums, &c->part,
+                    &c->Bhi, &c->Blo, &c->P, &c->wst, &c->wrawb, &c->rawb, &c->gerr,
+                    &c->mscale, &c->Jrowsum, &c->mmean, &c->swork};
   for (DevBuf *b : bufs)
     if (b->p) cudaFree(b->p);
+  for (auto &t : c->timed) {
+    cudaEventDestroy(t.second.first);
+    cudaEventDestroy(t.second.second);
+  }
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
   return J3G_OK;
@@ -477,6 +812,7 @@ int j3g_set_mesh(j3g_context *c, int nx, int ny, int nz, const double *xc, const
   J3G_CUDA(c, cudaStreamSynchronize(c->stream));
   c->mesh_set = true;
   c->bg_dirty = true;
+  drop_stored(c);  // the stored sensitivity belongs to the old geometry
   return J3G_OK;
 }
 
@@ -488,6 +824,7 @@ int j3g_set_background(j3g_context *c, int nbg, const double *thick) {
   J3G_TRY(upload(c, c->dbg, c->bg));
   J3G_CUDA(c, cudaStreamSynchronize(c->stream));
   c->bg_dirty = true;
+  drop_stored(c);  // the stored sensitivity belongs to the old geometry
   return J3G_OK;
 }
 
@@ -503,6 +840,7 @@ int j3g_set_stations(j3g_context *c, int n, const double *x, const double *y, co
   c->nmeas = n;
   c->stations_set = true;
   c->bg_dirty = true;
+  drop_stored(c);  // the stored sensitivity belongs to the old geometry
   return J3G_OK;
 }
 
@@ -514,6 +852,7 @@ int j3g_set_kind(j3g_context *c, int kind, double inc, double dec, double fs) {
   c->dec = dec;
   c->fs = fs;
   c->bg_dirty = true;
+  drop_stored(c);  // the stored sensitivity belongs to the old geometry
   if (c->transform != J3G_T_NONE) {
     const bool ok = (c->transform == J3G_T_FTG_INVARIANT && kind == J3G_TENSOR) ||
                     ((c->transform == J3G_T_TOTAL_FIELD || c->transform == J3G_T_TFA) &&
@@ -608,6 +947,145 @@ int j3g_lqderivative(j3g_context *c, const double *h_model, const double *h_misf
   return J3G_OK;
 }
 
+int j3g_build_sensitivity(j3g_context *c, int storage) {
+  if (!c) return J3G_ERR_ARG;
+  cudaSetDevice(c->device);
+  return build_stored(c, storage);
+}
+
+int j3g_drop_sensitivity(j3g_context *c) {
+  if (!c) return J3G_ERR_ARG;
+  cudaSetDevice(c->device);
+  drop_stored(c);
+  return J3G_OK;
+}
+
+int j3g_sensitivity_info(const j3g_context *c, int *storage, long long *rows, long long *cols,
+                         long long *bytes) {
+  if (!c) return J3G_ERR_ARG;
+  if (storage) *storage = c->storage;
+  if (rows) *rows = c->storage ? c->st_rows : 0;
+  if (cols) *cols = c->storage ? c->ngrid() : 0;
+  if (bytes)
+    *bytes = c->storage == J3G_STORE_FP32     ? c->st_rows * c->st_ld * 4
+             : c->storage == J3G_STORE_F16X2 ? 2 * (c->st_rows * c->st_ld * 2) + 2 * (c->ngrid() * c->st_ldT * 2)
+                                              : 0;
+  return J3G_OK;
+}
+
+int j3g_stored_forward_device(j3g_context *c, const double *d_model, double *d_data) {
+  if (!c || !d_model || !d_data) return fail(c, J3G_ERR_ARG, "null pointer");
+  cudaSetDevice(c->device);
+  J3G_TRY(check_stored(c));
+  if (c->storage == J3G_STORE_FP32) return stored_forward_f32(c, d_model, d_data, nullptr);
+  return batched_forward_impl(c, 1, d_model, d_data, nullptr);
+}
+
+int j3g_stored_lqderivative_device(j3g_context *c, const double *d_model, const double *d_misfit,
+                                   double *d_grad) {
+  if (!c || !d_model || !d_misfit || !d_grad) return fail(c, J3G_ERR_ARG, "null pointer");
+  cudaSetDevice(c->device);
+  J3G_TRY(check_stored(c));
+  if (c->storage == J3G_STORE_FP32) return stored_adjoint_f32(c, d_model, d_misfit, d_grad);
+  return batched_adjoint_impl(c, 1, d_model, d_misfit, d_grad);
+}
+
+int j3g_batched_forward_device(j3g_context *c, int nmodels, const double *d_models,
+                               double *d_data) {
+  if (!c || nmodels < 0 || (nmodels > 0 && (!d_models || !d_data)))
+    return fail(c, J3G_ERR_ARG, "bad batched arguments");
+  cudaSetDevice(c->device);
+  J3G_TRY(check_stored(c));
+  if (nmodels == 0) return J3G_OK;
+  return batched_forward_impl(c, nmodels, d_models, d_data, nullptr);
+}
+
+int j3g_batched_lqderivative_device(j3g_context *c, int nmodels, const double *d_models,
+                                    const double *d_misfits, double *d_grads) {
+  if (!c || nmodels < 0 || (nmodels > 0 && (!d_models || !d_misfits || !d_grads)))
+    return fail(c, J3G_ERR_ARG, "bad batched arguments");
+  cudaSetDevice(c->device);
+  J3G_TRY(check_stored(c));
+  if (nmodels == 0) return J3G_OK;
+  return batched_adjoint_impl(c, nmodels, d_models, d_misfits, d_grads);
+}
+
+int j3g_batched_forward(j3g_context *c, int nmodels, const double *h_models, double *h_data) {
+  if (!c || nmodels < 0 || (nmodels > 0 && (!h_models || !h_data)))
+    return fail(c, J3G_ERR_ARG, "bad batched arguments");
+  cudaSetDevice(c->device);
+  J3G_TRY(check_stored(c));
+  if (nmodels == 0) return J3G_OK;
+  const size_t nm = (size_t)nmodels * c->nparm(), nd = (size_t)nmodels * c->nmeas * c->dpm();
+  J3G_TRY(ensure(c, c->model, sizeof(double) * nm));
+  J3G_TRY(ensure(c, c->data, sizeof(double) * nd));
+  J3G_CUDA(c, cudaMemcpyAsync(c->model.p, h_models, sizeof(double) * nm, cudaMemcpyHostToDevice,
+                              c->stream));
+  J3G_TRY(batched_forward_impl(c, nmodels, ptr<double>(c->model), ptr<double>(c->data), nullptr));
+  J3G_CUDA(c, cudaMemcpyAsync(h_data, c->data.p, sizeof(double) * nd, cudaMemcpyDeviceToHost,
+                              c->stream));
+  J3G_CUDA(c, cudaStreamSynchronize(c->stream));
+  return check_gemm_flag(c);
+}
+
+int j3g_batched_lqderivative(j3g_context *c, int nmodels, const double *h_models,
+                             const double *h_misfits, double *h_grads) {
+  if (!c || nmodels < 0 || (nmodels > 0 && (!h_models || !h_misfits || !h_grads)))
+    return fail(c, J3G_ERR_ARG, "bad batched arguments");
+  cudaSetDevice(c->device);
+  J3G_TRY(check_stored(c));
+  if (nmodels == 0) return J3G_OK;
+  const size_t nm = (size_t)nmodels * c->nparm(), nd = (size_t)nmodels * c->nmeas * c->dpm();
+  J3G_TRY(ensure(c, c->model, sizeof(double) * nm));
+  J3G_TRY(ensure(c, c->misfit, sizeof(double) * nd));
+  J3G_TRY(ensure(c, c->grad, sizeof(double) * nm));
+  J3G_CUDA(c, cudaMemcpyAsync(c->model.p, h_models, sizeof(double) * nm, cudaMemcpyHostToDevice,
+                              c->stream));
+  J3G_CUDA(c, cudaMemcpyAsync(c->misfit.p, h_misfits, sizeof(double) * nd,
+                              cudaMemcpyHostToDevice, c->stream));
+  J3G_TRY(batched_adjoint_impl(c, nmodels, ptr<double>(c->model), ptr<double>(c->misfit),
+                               ptr<double>(c->grad)));
+  J3G_CUDA(c, cudaMemcpyAsync(h_grads, c->grad.p, sizeof(double) * nm, cudaMemcpyDeviceToHost,
+                              c->stream));
+  J3G_CUDA(c, cudaStreamSynchronize(c->stream));
+  return check_gemm_flag(c);
+}
+
+static void clear_timing(j3g_context *c) {
+  for (auto &t : c->timed) {
+    cudaEventDestroy(t.second.first);
+    cudaEventDestroy(t.second.second);
+  }
+  c->timed.clear();
+}
+
+int j3g_set_timing(j3g_context *c, int enable) {
+  if (!c) return J3G_ERR_ARG;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  clear_timing(c);
+  c->timing = enable != 0;
+  return J3G_OK;
+}
+
+int j3g_get_timing(j3g_context *c, int category, double *total_ms, long long *launches) {
+  if (!c || !total_ms || !launches) return J3G_ERR_ARG;
+  cudaSetDevice(c->device);
+  J3G_CUDA(c, cudaStreamSynchronize(c->stream));
+  double ms = 0.0;
+  long long n = 0;
+  for (auto &t : c->timed) {
+    if (t.first != category) continue;
+    float v = 0.0f;
+    J3G_CUDA(c, cudaEventElapsedTime(&v, t.second.first, t.second.second));
+    ms += v;
+    ++n;
+  }
+  *total_ms = ms;
+  *launches = n;
+  return J3G_OK;
+}
+
 int j3g_launch_count(const j3g_context *c, long long *count) {
   if (!c || !count) return J3G_ERR_ARG;
   *count = c->launches;
@@ -618,7 +1096,7 @@ int j3g_synchronize(j3g_context *c) {
   if (!c) return J3G_ERR_ARG;
   cudaSetDevice(c->device);
   J3G_CUDA(c, cudaStreamSynchronize(c->stream));
-  return J3G_OK;
+  return check_gemm_flag(c);
 }
 
 int j3g_probe_fp64(j3g_context *c, double *gflops) {

@@ -1,0 +1,431 @@
+// gemm_tc.cu -- batched sensitivity products on the 5th-generation tensor
+// cores (tcgen05 + TMA + TMEM) with FP64-class accuracy from 16-bit inputs.
+//
+//   P[split][n][m] = sum_{k in split} (Ahi Bhi + Ahi Blo + Alo Bhi)[m][k][n]
+//
+// A [M][K] and B [N][K] are K-major fp16 (or bf16) hi / lo pairs, rows padded
+// to a multiple of 64 elements.  Forward: A = J (rows x cells), B = models;
+// adjoint: A = J^T (cells x rows), B = scaled residuals.
+//
+// Accuracy.  The tensor core's FP32 accumulation loses about 2e-8 relative
+// per MMA step, growing linearly with the number of steps that feed one
+// accumulator.  So the hi*hi products of every kStepsPerDrain MMA steps (32
+// cells) go to a fresh TMEM accumulator (double-buffered, A0 / A1) that the
+// drain warps add, with round-to-nearest FP32 adds, into sums held in
+// registers while the next steps are multiplied; the cross terms hi*lo +
+// lo*hi, about 2^-11 of the total, accumulate in a third TMEM region (X) for
+// the whole split.  Splits of at most 64 k-blocks keep the register sums
+// short; the caller adds the splits in FP64.
+//
+// One CTA computes a 128 x BN tile of one K split with 10 warps:
+//   warp 0      TMA producer (Ahi, Alo, Bhi, Blo per stage, 128-byte swizzle)
+//   warp 1      TMEM allocation; lane 0 issues the MMAs
+//   warps 2-9   drain: warp w reads TMEM lanes 32*(w%4).. and columns
+//               (w-2)/4 * BN/2 .. + BN/2, sums them per k-block, writes the tile
+// Every mbarrier wait is bounded by a %globaltimer deadline; on expiry the
+// CTA records an error code, stops issuing, drains what it issued (again
+// bounded), frees its TMEM and returns.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "stored.h"
+
+namespace j3g {
+namespace {
+
+constexpr int BM = 128;
+constexpr int BK = 64;  // 16-bit elements per 128-byte swizzled row
+constexpr int kGemmThreads = 320;
+constexpr int kDrainWarps = 8;
+// hi*hi MMA steps (16 products each) per TMEM accumulator before it is
+// drained into the register sums; 2 halves the tensor-core rounding of 4
+constexpr int kStepsPerDrain = 2;
+constexpr int kDrainsPerBlock = (BK / 16) / kStepsPerDrain;
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
+
+template <int BN, bool F16> struct Cfg {
+  static constexpr int STAGES = BN == 128 ? 3 : 4;
+  static constexpr int A_BYTES = BM * BK * 2;
+  static constexpr int B_BYTES = BN * BK * 2;
+  static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
+  static constexpr int NBAR = 2 * STAGES + 5;  // full, empty, A full x2, A empty x2, X full
+  static constexpr int SMEM = STAGES * STAGE_BYTES + NBAR * 8 + 16 + 1024;
+  static constexpr uint32_t TMEM_COLS = 4 * BN;  // A0, A1, X (+ unused), power of two
+  // kind::f16 instruction descriptor: D F32 (bit 4), A and B format at bits
+  // 7 and 10 (0 = F16, 1 = BF16), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+  static constexpr uint32_t FMT = F16 ? 0u : 1u;
+  static constexpr uint32_t IDESC = (1u << 4) | (FMT << 7) | (FMT << 10) |
+                                    ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+  static constexpr int COLS_PER_WARP = BN / 2;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ unsigned long long now_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: true when the phase completed, false after the deadline.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = now_ns();
+  while (true) {
+    if (mbar_try(bar, parity)) return true;
+    if (now_ns() - t0 > kWaitNs) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// UMMA shared-memory descriptor of a K-major tile stored with the 128-byte
+// swizzle (rows of 128 B, 8-row atoms 1024 B apart): start address >> 4 in
+// bits 0-13, leading offset 16 B (unused for this layout) in bits 16-29,
+// stride offset 1024 B in bits 32-45, the fixed 0b001 in bits 46-48, base
+// offset 0 (atoms 1024-byte aligned), swizzle mode 2 (128 B) in bits 61-63.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void umma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                     uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// 16 consecutive FP32 columns of this warp's 32 TMEM lanes (one per thread).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+
+template <int BN, bool F16>
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    k_gemm_x3(const __grid_constant__ CUtensorMap tmAhi, const __grid_constant__ CUtensorMap tmAlo,
+              const __grid_constant__ CUtensorMap tmBhi, const __grid_constant__ CUtensorMap tmBlo,
+              int kb_per_split, int kb_total, int M, int N, float *__restrict__ P, long long ldp,
+              long long slice, int *__restrict__ err) {
+  using C = Cfg<BN, F16>;
+  constexpr int S = C::STAGES;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                              ~static_cast<uintptr_t>(1023));
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * C::STAGE_BYTES);
+  uint64_t *full = bars, *empty = bars + S;
+  uint64_t *a_full = bars + 2 * S, *a_empty = bars + 2 * S + 2, *x_full = bars + 2 * S + 4;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + C::NBAR);
+  volatile int *fail = reinterpret_cast<volatile int *>(tmem_slot + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;  // N tiles fastest (see launch_bn)
+  const int kb0 = blockIdx.z * kb_per_split;
+  const int nkb = min(kb_total, kb0 + kb_per_split) - kb0;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 2 * S; ++s) mbar_init(smem_u32(bars + s), 1);
+    mbar_init(smem_u32(a_full), 1);
+    mbar_init(smem_u32(a_full + 1), 1);
+    mbar_init(smem_u32(a_empty), kDrainWarps);
+    mbar_init(smem_u32(a_empty + 1), kDrainWarps);
+    mbar_init(smem_u32(x_full), 1);
+    *fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmAhi)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmAlo)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmBhi)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmBlo)) : "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(C::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t tmemA[2] = {tmem, tmem + (uint32_t)BN};
+  const uint32_t tmemX = tmem + 2u * BN;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int issued = 0;
+      for (int i = 0; i < nkb; ++i) {
+        const int s = i % S;
+        const uint32_t ph = (uint32_t)(i / S) & 1u;
+        if (i >= S && !mbar_wait(smem_u32(empty + s), ph ^ 1u)) {
+          atomicExch(err, 1);
+          *fail = 1;
+          break;
+        }
+        if (*fail) break;
+        uint8_t *st = smem + s * C::STAGE_BYTES;
+        const uint32_t fb = smem_u32(full + s);
+        mbar_expect_tx(fb, (uint32_t)C::STAGE_BYTES);
+        const int kx = (kb0 + i) * BK;
+        tma_load_2d(smem_u32(st), &tmAhi, kx, m0, fb);
+        tma_load_2d(smem_u32(st + C::A_BYTES), &tmAlo, kx, m0, fb);
+        tma_load_2d(smem_u32(st + 2 * C::A_BYTES), &tmBhi, kx, n0, fb);
+        tma_load_2d(smem_u32(st + 2 * C::A_BYTES + C::B_BYTES), &tmBlo, kx, n0, fb);
+        issued = i + 1;
+      }
+      // the last stages may still be landing; let them complete (bounded)
+      for (int i = (issued > S ? issued - S : 0); i < issued; ++i)
+        mbar_wait(smem_u32(full + (i % S)), (uint32_t)(i / S) & 1u);
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      bool ok = true;
+      for (int i = 0; i < nkb && ok; ++i) {
+        const int s = i % S;
+        if (!mbar_wait(smem_u32(full + s), (uint32_t)(i / S) & 1u)) {
+          atomicExch(err, 2);
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t base = smem_u32(smem + s * C::STAGE_BYTES);
+        const uint32_t ahi = base, alo = base + C::A_BYTES;
+        const uint32_t bhi = base + 2 * C::A_BYTES, blo = bhi + C::B_BYTES;
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; ++kk) {
+          const int d = i * kDrainsPerBlock + kk / kStepsPerDrain;  // drain index
+          const int b = d & 1;
+          if (kk % kStepsPerDrain == 0 && d >= 2 &&
+              !mbar_wait(smem_u32(a_empty + b), ((uint32_t)(d >> 1) & 1u) ^ 1u)) {
+            // the buffer of drain d-2 was never emptied
+            atomicExch(err, 3);
+            ok = false;
+            break;
+          }
+          if (kk % kStepsPerDrain == 0) tc_fence_after();
+          const uint32_t off = kk * 32;  // 16 elements = 32 bytes along K inside the swizzle atom
+          const uint64_t dah = sw128_desc(ahi + off), dal = sw128_desc(alo + off);
+          const uint64_t dbh = sw128_desc(bhi + off), dbl = sw128_desc(blo + off);
+          umma(tmemA[b], dah, dbh, C::IDESC, (kk % kStepsPerDrain) > 0 ? 1u : 0u);
+          umma(tmemX, dah, dbl, C::IDESC, (i > 0 || kk > 0) ? 1u : 0u);
+          umma(tmemX, dal, dbh, C::IDESC, 1u);
+          if ((kk + 1) % kStepsPerDrain == 0)
+            umma_commit(smem_u32(a_full + b));  // this drain's hi*hi ready
+        }
+        if (!ok) break;
+        umma_commit(smem_u32(empty + s));  // smem stage free once these MMAs finish
+      }
+      if (ok) {
+        umma_commit(smem_u32(x_full));  // cross terms complete
+      } else {
+        *fail = 1;
+      }
+    }
+  } else {
+    // ---------------- drain warps ----------------
+    const int q = warp & 3;                                   // TMEM lane quarter
+    const int ch = (warp - 2) >> 2;                           // column half
+    const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+    const uint32_t col0 = (uint32_t)(ch * C::COLS_PER_WARP);
+    float s[C::COLS_PER_WARP];  // round-to-nearest FP32 sums of the drained k-blocks
+#pragma unroll
+    for (int j = 0; j < C::COLS_PER_WARP; ++j) s[j] = 0.0f;
+    bool ok = true;
+    for (int i = 0; i < nkb * kDrainsPerBlock; ++i) {  // i = drain index
+      const int b = i & 1;
+      bool got = mbar_wait(smem_u32(a_full + b), (uint32_t)(i >> 1) & 1u);
+      got = __all_sync(0xffffffffu, got ? 1 : 0) != 0;
+      if (!got) {
+        if (lane == 0) atomicExch(err, 4);
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+#pragma unroll
+      for (int h = 0; h < C::COLS_PER_WARP / 16; ++h) {
+        uint32_t v[16];
+        tmem_ld16(tmemA[b] + lane_off + col0 + 16u * h, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) s[16 * h + j] = __fadd_rn(s[16 * h + j], __uint_as_float(v[j]));
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(a_empty + b));
+    }
+    if (ok) {
+      bool got = nkb > 0 && mbar_wait(smem_u32(x_full), 0u);
+      got = __all_sync(0xffffffffu, got ? 1 : 0) != 0;
+      if (got) {
+        tc_fence_after();
+#pragma unroll
+        for (int h = 0; h < C::COLS_PER_WARP / 16; ++h) {
+          uint32_t v[16];
+          tmem_ld16(tmemX + lane_off + col0 + 16u * h, v);
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            s[16 * h + j] = __fadd_rn(s[16 * h + j], __uint_as_float(v[j]));
+        }
+      } else if (nkb > 0) {
+        if (lane == 0) atomicExch(err, 5);
+      }
+    }
+    const int row = m0 + q * 32 + lane;
+    float *out = P + (long long)blockIdx.z * slice;
+    if (row < M) {
+#pragma unroll
+      for (int j = 0; j < C::COLS_PER_WARP; ++j) {
+        const int n = n0 + (int)col0 + j;
+        if (n < N) out[(long long)n * ldp + row] = s[j];
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(C::TMEM_COLS)
+                 : "memory");
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// 2-D K-major 16-bit map: rows x ld elements (ld multiple of 64), box BK x box_rows.
+bool make_map(CUtensorMap *map, const void *base, long long rows, long long ld, int box_rows,
+              bool f16) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  return fn(map, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+            const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN, bool F16>
+cudaError_t launch_bn(const GemmOperands &g, int nsplit, float *P, long long ldp, long long slice,
+                      int *err, cudaStream_t st) {
+  CUtensorMap ah, al, bh, bl;
+  if (!make_map(&ah, g.a_hi, g.m, g.ld, BM, F16) || !make_map(&al, g.a_lo, g.m, g.ld, BM, F16) ||
+      !make_map(&bh, g.b_hi, g.n_pad, g.ld, BN, F16) ||
+      !make_map(&bl, g.b_lo, g.n_pad, g.ld, BN, F16))
+    return cudaErrorInvalidValue;
+  const int kb_total = (int)(g.ld / BK);
+  const int kb_per = (kb_total + nsplit - 1) / nsplit;
+  const int nsp = (kb_total + kb_per - 1) / kb_per;
+  cudaError_t e = cudaFuncSetAttribute(k_gemm_x3<BN, F16>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       Cfg<BN, F16>::SMEM);
+  if (e != cudaSuccess) return e;
+  // N tiles vary fastest so the CTAs sharing an A tile run side by side (L2 reuse)
+  dim3 grid((unsigned)(g.n_pad / BN), (unsigned)((g.m + BM - 1) / BM), (unsigned)nsp);
+  k_gemm_x3<BN, F16><<<grid, kGemmThreads, Cfg<BN, F16>::SMEM, st>>>(
+      ah, al, bh, bl, kb_per, kb_total, (int)g.m, (int)g.n, P, ldp, slice, err);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int gemm_n_tile(int n) { return n <= 64 ? 64 : 128; }
+
+int gemm_splits_used(long long ld, int nsplit) {
+  const int kb_total = (int)(ld / BK);
+  const int kb_per = (kb_total + nsplit - 1) / nsplit;
+  return (kb_total + kb_per - 1) / kb_per;
+}
+
+cudaError_t launch_gemm_x3(const GemmOperands &g, int nsplit, float *P, long long ldp,
+                           long long slice, int *err, cudaStream_t st) {
+  if (g.ld % BK != 0 || g.n_pad % gemm_n_tile((int)g.n) != 0) return cudaErrorInvalidValue;
+  if ((reinterpret_cast<uintptr_t>(g.a_hi) | reinterpret_cast<uintptr_t>(g.a_lo) |
+       reinterpret_cast<uintptr_t>(g.b_hi) | reinterpret_cast<uintptr_t>(g.b_lo)) & 15)
+    return cudaErrorMisalignedAddress;
+  const int nt = gemm_n_tile((int)g.n);
+  if (g.f16) {
+    if (nt == 64) return launch_bn<64, true>(g, nsplit, P, ldp, slice, err, st);
+    return launch_bn<128, true>(g, nsplit, P, ldp, slice, err, st);
+  }
+  if (nt == 64) return launch_bn<64, false>(g, nsplit, P, ldp, slice, err, st);
+  return launch_bn<128, false>(g, nsplit, P, ldp, slice, err, st);
+}
+
+}  // namespace j3g

@@ -433,6 +433,50 @@ __global__ void __launch_bounds__(kThreads)
   for (int r = 0; r < RAW; ++r) rows[((long long)sl * RAW + r) * ld + cell] = raw[r];
 }
 
+// Stored rows for the device-resident sensitivity: the node components of the
+// kind (scalar 1, tensor 6, joint 7) or the 3 raw magnetic rows, one row per
+// (station, stored component), written as OutT (double or float).
+template <int KIND> struct StoredRows {
+  static constexpr int n = (KIND == KIND_MAGNETIC) ? 3 : KindTraits<KIND>::ncomp;
+};
+
+template <int KIND, class OutT>
+__global__ void __launch_bounds__(kThreads)
+    k_cell_stored(MeshView m, const double *__restrict__ F, MagField mf, OutT *__restrict__ rows,
+                  long long ld) {
+  constexpr int NCMP = KindTraits<KIND>::ncomp;
+  constexpr int OFF = Slots<KIND>::off;
+  constexpr int NS = StoredRows<KIND>::n;
+  const long long cell = (long long)blockIdx.x * kThreads + threadIdx.x;
+  const int sl = blockIdx.y;
+  if (cell >= m.ngrid()) return;
+  const int k = cell % m.nz;
+  const long long t = cell / m.nz;
+  const int j = t % m.ny;
+  const int i = t / m.ny;
+  const int ny1 = m.ny + 1, nz1 = m.nz + 1;
+  const int nn = (m.nx + 1) * ny1 * nz1;
+  double u[NC_COUNT];
+#pragma unroll
+  for (int q = 0; q < NCMP; ++q) {
+    const double *f = F + ((long long)sl * NCMP + q) * nn;
+    double v[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      v[c] = f[((i + ((c >> 2) & 1)) * ny1 + (j + ((c >> 1) & 1))) * nz1 + (k + (c & 1))];
+    u[q + OFF] = combine8(q + OFF, v);
+  }
+  if (KIND == KIND_MAGNETIC) {
+    double raw[10];
+    raw_from_comps(KIND, u, mf, raw);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) rows[((long long)sl * NS + r) * ld + cell] = (OutT)raw[r];
+  } else {
+#pragma unroll
+    for (int q = 0; q < NCMP; ++q) rows[((long long)sl * NS + q) * ld + cell] = (OutT)u[q + OFF];
+  }
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(kThreads)
     k_cell_direct(MeshView m, StationView st, int s0, MagField mf, double *__restrict__ rows,
@@ -606,6 +650,25 @@ cudaError_t launch_sens_rows(int kind, bool node_exact, const MeshView &m, const
   } else {
     dim3 g2(cdiv(m.ngrid(), kThreads), ns);
     J3G_DISPATCH(kind, (k_cell_direct<K><<<g2, kThreads, 0, st>>>(m, s, s0, mf, rows, ld)));
+  }
+  return cudaGetLastError();
+}
+
+int stored_rows_per_station(int kind) {
+  return kind == KIND_MAGNETIC ? 3 : kind_ncomp(kind);
+}
+
+cudaError_t launch_stored_rows(int kind, const MeshView &m, const StationView &s, int s0, int ns,
+                               const MagField &mf, double *F, double *rows64, float *rows32,
+                               long long ld, cudaStream_t st) {
+  dim3 g1(cdiv(m.nnodes(), kThreads), ns);
+  dim3 g2(cdiv(m.ngrid(), kThreads), ns);
+  if (rows64) {
+    J3G_DISPATCH(kind, (k_node_eval<K><<<g1, kThreads, 0, st>>>(m, s, s0, F),
+                        k_cell_stored<K, double><<<g2, kThreads, 0, st>>>(m, F, mf, rows64, ld)));
+  } else {
+    J3G_DISPATCH(kind, (k_node_eval<K><<<g1, kThreads, 0, st>>>(m, s, s0, F),
+                        k_cell_stored<K, float><<<g2, kThreads, 0, st>>>(m, F, mf, rows32, ld)));
   }
   return cudaGetLastError();
 }

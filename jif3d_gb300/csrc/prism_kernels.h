@@ -78,6 +78,15 @@ cudaError_t launch_background_grad(int kind, int nmeas, int nbg, const double *w
 cudaError_t launch_sens_rows(int kind, bool node_exact, const MeshView &m,
                              const StationView &s, int s0, int ns, const MagField &mf,
                              double *F, double *rows, long long ld, cudaStream_t st);
+// Rows of the device-resident sensitivity for stations s0..s0+ns-1: per
+// station the kind's node components (scalar 1, tensor 6 = xx yy zz xy xz yz,
+// joint 7 = gz + tensor) or, for magnetics, the 3 raw rows Bx By Bz.  Written
+// as double (rows64) or float (rows32), row (sl*nstored + q) at stride ld.
+int stored_rows_per_station(int kind);
+cudaError_t launch_stored_rows(int kind, const MeshView &m, const StationView &s, int s0, int ns,
+                               const MagField &mf, double *F, double *rows64, float *rows32,
+                               long long ld, cudaStream_t st);
+
 // d[(s0+sl)*raw + r] = sum_cell rows[(sl*raw + r)*ld + cell] * rho[cell]
 cudaError_t launch_rows_dot(int raw, int ns, long long ngrid, const double *rows, long long ld,
                             const double *rho, double *out, cudaStream_t st);

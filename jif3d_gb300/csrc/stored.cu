@@ -1,0 +1,554 @@
+// stored.cu -- the device-resident sensitivity matrix and its HBM-streaming
+// products (the GPU counterpart of FullSensitivityGravMagCalculator's cached
+// path, GravMag/FullSensitivityGravMagCalculator.h:136-221: d = J m and
+// g = 2 J^T r without recomputing any box term).
+//
+// Storage: row-major J (rows = station x stored component, columns = cells,
+// padded to a multiple of 64 columns with zeros), as
+//   FP32                       4 B per element, or
+//   FP16 hi + lo, row scale    2 x 2 B per element: J[r][c] ~= s_r (hi + lo),
+//                              s_r a power of two with max|J/s_r| in (2^13, 2^14],
+//                              hi = fp16(J/s_r), lo = fp16(J/s_r - hi) (22
+//                              significant bits), plus the transposed copy
+//                              used as the K-major operand of the adjoint GEMM.
+// Streaming products accumulate in FP32 in short chains and in FP64 across
+// chains; the tensor-core products are in gemm_tc.cu.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "stored.h"
+
+namespace j3g {
+namespace {
+
+constexpr int kT = 256;
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int NT>
+__device__ __forceinline__ double block_sum_d(double v, double *red) {
+  v = warp_sum_d(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int w = 0; w < NT / 32; ++w) r += red[w];
+    red[0] = r;
+  }
+  __syncthreads();
+  r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ double warp_max_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Power-of-two scale that brings max|v| into (2^13, 2^14]: the fp16 parts
+// of v / scale stay far from overflow and mostly above the subnormal range,
+// and dividing by it is exact.
+__device__ __forceinline__ double pow2_scale(double maxabs) {
+  if (!(maxabs > 0.0)) return 1.0;
+  int e;
+  frexp(maxabs, &e);  // maxabs in [2^(e-1), 2^e)
+  return ldexp(1.0, e - 14);
+}
+
+__device__ __forceinline__ void split_half(double v, __half &h, __half &l) {
+  h = __double2half(v);
+  l = __double2half(v - (double)__half2float(h));
+}
+
+template <class T>
+__device__ __forceinline__ double block_max_abs(const T &get, long long n, double *red) {
+  double m = 0.0;
+  for (long long c = threadIdx.x; c < n; c += kT) m = fmax(m, fabs(get(c)));
+  m = warp_max_d(m);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double mm = 0.0;
+    for (int w = 0; w < kT / 32; ++w) mm = fmax(mm, red[w]);
+    red[0] = mm;
+  }
+  __syncthreads();
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// One block per row: power-of-two row scale and fp16 hi / lo split of an FP64
+// row (padding columns zero).  scale[row0 + r] receives the scale and, when
+// given, rowsum[row0 + r] the FP64 sum of the row (J 1, used to add back the
+// mean of a centred model).
+__global__ void k_split_rows(const double *__restrict__ rows, long long ld_in, long long ncol,
+                             __half *__restrict__ hi, __half *__restrict__ lo, long long ld_out,
+                             float *__restrict__ scale, double *__restrict__ rowsum,
+                             long long row0) {
+  const long long r = blockIdx.x;
+  const double *p = rows + r * ld_in;
+  __shared__ double red[kT / 32];
+  const double sc = pow2_scale(block_max_abs([&](long long c) { return p[c]; }, ncol, red));
+  if (threadIdx.x == 0) scale[row0 + r] = (float)sc;
+  if (rowsum) {
+    double acc = 0.0;
+    for (long long c = threadIdx.x; c < ncol; c += kT) acc += p[c];
+    acc = block_sum_d<kT>(acc, red);
+    if (threadIdx.x == 0) rowsum[row0 + r] = acc;
+  }
+  const double inv = 1.0 / sc;
+  __half *h = hi + (row0 + r) * ld_out;
+  __half *l = lo + (row0 + r) * ld_out;
+  for (long long c = threadIdx.x; c < ld_out; c += kT) {
+    __half hv, lv;
+    split_half(c < ncol ? p[c] * inv : 0.0, hv, lv);
+    h[c] = hv;
+    l[c] = lv;
+  }
+}
+
+// 32x32 tiled transpose of a 16-bit matrix [rows][ld_in] -> [cols][ld_out].
+__global__ void k_transpose16(const uint16_t *__restrict__ in, long long ld_in, long long rows,
+                              long long cols, uint16_t *__restrict__ out, long long ld_out) {
+  __shared__ uint16_t tile[32][34];
+  const long long c0 = (long long)blockIdx.x * 32, r0 = (long long)blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  for (int k = ty; k < 32; k += 8) {
+    const long long r = r0 + k, c = c0 + tx;
+    tile[k][tx] = (r < rows && c < cols) ? in[r * ld_in + c] : (uint16_t)0;
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const long long c = c0 + k, r = r0 + tx;
+    if (c < cols && r < ld_out) out[c * ld_out + r] = tile[tx][k];
+  }
+}
+
+// Splitting an FP64 matrix [nrow][ld_src] (rows = models or residual vectors)
+// into fp16 hi / lo rows [nrow_pad][ld_dst], in three grid-wide passes so that
+// a few hundred long rows still fill the GPU:
+//   k_row_stats     per (row, column chunk): max |v| and sum v
+//   k_row_finalize  per row: power-of-two scale, optional mean (centring)
+//   k_split_chunks  per (row, column chunk): (v - mean) / scale -> hi + lo
+// v = src[r][c] * colscale[c] (colscale optional).
+constexpr int kChunk = 8192;
+
+__device__ __forceinline__ double scaled_val(const double *src, long long ld_src, int nrow,
+                                             long long ncol, const float *colscale, long long r,
+                                             long long c) {
+  if (r >= nrow || c >= ncol) return 0.0;
+  const double v = src[r * ld_src + c];
+  return colscale ? v * (double)colscale[c] : v;
+}
+
+__global__ void k_row_stats(const double *__restrict__ src, long long ld_src, int nrow,
+                            long long ncol, const float *__restrict__ colscale,
+                            double *__restrict__ part_max, double *__restrict__ part_sum,
+                            int nchunk) {
+  const long long r = blockIdx.y;
+  const long long c0 = (long long)blockIdx.x * kChunk;
+  double m = 0.0, sum = 0.0;
+  for (long long c = c0 + threadIdx.x; c < c0 + kChunk; c += kT) {
+    const double v = scaled_val(src, ld_src, nrow, ncol, colscale, r, c);
+    m = fmax(m, fabs(v));
+    sum += v;
+  }
+  __shared__ double red[kT / 32];
+  m = warp_max_d(m);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double mm = 0.0;
+    for (int w = 0; w < kT / 32; ++w) mm = fmax(mm, red[w]);
+    part_max[r * nchunk + blockIdx.x] = mm;
+  }
+  __syncthreads();
+  sum = block_sum_d<kT>(sum, red);
+  if (threadIdx.x == 0) part_sum[r * nchunk + blockIdx.x] = sum;
+}
+
+__global__ void k_row_finalize(int nrow_pad, int nchunk, long long ncol, bool center,
+                               const double *__restrict__ part_max,
+                               const double *__restrict__ part_sum, float *__restrict__ rowscale,
+                               double *__restrict__ rowmean) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrow_pad) return;
+  double mx = 0.0, sum = 0.0;
+  for (int k = 0; k < nchunk; ++k) {
+    mx = fmax(mx, part_max[(long long)r * nchunk + k]);
+    sum += part_sum[(long long)r * nchunk + k];
+  }
+  const double mean = (center && ncol > 0) ? sum / (double)ncol : 0.0;
+  // |v - mean| <= max|v| + |mean| <= 2 max|v|
+  rowscale[r] = (float)pow2_scale(center ? 2.0 * mx : mx);
+  if (rowmean) rowmean[r] = mean;
+}
+
+__global__ void k_split_chunks(const double *__restrict__ src, long long ld_src, int nrow,
+                               long long ncol, const float *__restrict__ colscale,
+                               const float *__restrict__ rowscale,
+                               const double *__restrict__ rowmean, __half *__restrict__ hi,
+                               __half *__restrict__ lo, long long ld_dst) {
+  const long long r = blockIdx.y;
+  const long long c0 = (long long)blockIdx.x * kChunk;
+  const double inv = 1.0 / (double)rowscale[r];
+  const double mean = rowmean ? rowmean[r] : 0.0;
+  for (long long c = c0 + threadIdx.x; c < c0 + kChunk && c < ld_dst; c += kT) {
+    const double v = (r < nrow && c < ncol)
+                         ? (scaled_val(src, ld_src, nrow, ncol, colscale, r, c) - mean) * inv
+                         : 0.0;
+    __half hv, lv;
+    split_half(v, hv, lv);
+    hi[r * ld_dst + c] = hv;
+    lo[r * ld_dst + c] = lv;
+  }
+}
+
+__global__ void k_to_f32(const double *__restrict__ src, long long n, long long npad,
+                         float *__restrict__ dst) {
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < npad;
+       t += (long long)gridDim.x * blockDim.x)
+    dst[t] = t < n ? (float)src[t] : 0.0f;
+}
+
+// d[r] = sum_c J[r][c] x[c]; one block per row, float4 streaming loads,
+// FP32 chains of 16 flushed into an FP64 sum.
+__global__ void __launch_bounds__(kT) k_gemv_f32(const float *__restrict__ J, long long ld,
+                                                 const float *__restrict__ x,
+                                                 double *__restrict__ out) {
+  const long long r = blockIdx.x;
+  const float4 *p = reinterpret_cast<const float4 *>(J + r * ld);
+  const float4 *xv = reinterpret_cast<const float4 *>(x);
+  const long long n4 = ld / 4;
+  double accd = 0.0;
+  long long i = threadIdx.x;
+  for (; i + 3 * kT < n4; i += 4 * kT) {
+    float4 a0 = __ldcs(p + i), a1 = __ldcs(p + i + kT), a2 = __ldcs(p + i + 2 * kT),
+           a3 = __ldcs(p + i + 3 * kT);
+    float4 b0 = xv[i], b1 = xv[i + kT], b2 = xv[i + 2 * kT], b3 = xv[i + 3 * kT];
+    float acc = a0.x * b0.x;
+    acc = fmaf(a0.y, b0.y, acc); acc = fmaf(a0.z, b0.z, acc); acc = fmaf(a0.w, b0.w, acc);
+    acc = fmaf(a1.x, b1.x, acc); acc = fmaf(a1.y, b1.y, acc); acc = fmaf(a1.z, b1.z, acc);
+    acc = fmaf(a1.w, b1.w, acc); acc = fmaf(a2.x, b2.x, acc); acc = fmaf(a2.y, b2.y, acc);
+    acc = fmaf(a2.z, b2.z, acc); acc = fmaf(a2.w, b2.w, acc); acc = fmaf(a3.x, b3.x, acc);
+    acc = fmaf(a3.y, b3.y, acc); acc = fmaf(a3.z, b3.z, acc); acc = fmaf(a3.w, b3.w, acc);
+    accd += (double)acc;
+  }
+  for (; i < n4; i += kT) {
+    const float4 a = __ldcs(p + i), b = xv[i];
+    float acc = a.x * b.x;
+    acc = fmaf(a.y, b.y, acc); acc = fmaf(a.z, b.z, acc); acc = fmaf(a.w, b.w, acc);
+    accd += (double)acc;
+  }
+  __shared__ double red[kT / 32];
+  accd = block_sum_d<kT>(accd, red);
+  if (threadIdx.x == 0) out[r] = accd;
+}
+
+// part[chunk][c] = sum_{r in chunk} J[r][c] w[r]; block = 1024 columns x RC rows.
+constexpr int kRC = 128;
+__global__ void __launch_bounds__(kT) k_gemv_t_f32(const float *__restrict__ J, long long ld,
+                                                   int nrows, const double *__restrict__ w,
+                                                   double *__restrict__ part) {
+  const long long c4 = (long long)blockIdx.x * kT + threadIdx.x;  // float4 column index
+  const int chunk = blockIdx.y;
+  const int r0 = chunk * kRC, r1 = min(nrows, r0 + kRC);
+  __shared__ float ws[kRC];
+  for (int t = threadIdx.x; t < kRC; t += kT) ws[t] = (r0 + t < r1) ? (float)w[r0 + t] : 0.0f;
+  __syncthreads();
+  if (c4 * 4 >= ld) return;
+  double d0 = 0, d1 = 0, d2 = 0, d3 = 0;
+  float f0 = 0, f1 = 0, f2 = 0, f3 = 0;
+  int cnt = 0;
+  for (int r = r0; r < r1; ++r) {
+    const float4 a = __ldcs(reinterpret_cast<const float4 *>(J + (long long)r * ld) + c4);
+    const float wr = ws[r - r0];
+    f0 = fmaf(a.x, wr, f0);
+    f1 = fmaf(a.y, wr, f1);
+    f2 = fmaf(a.z, wr, f2);
+    f3 = fmaf(a.w, wr, f3);
+    if (++cnt == 16) {
+      d0 += f0; d1 += f1; d2 += f2; d3 += f3;
+      f0 = f1 = f2 = f3 = 0.0f;
+      cnt = 0;
+    }
+  }
+  d0 += f0; d1 += f1; d2 += f2; d3 += f3;
+  double *o = part + (long long)chunk * ld + c4 * 4;
+  o[0] = d0; o[1] = d1; o[2] = d2; o[3] = d3;
+}
+
+__global__ void k_sum_parts(const double *__restrict__ part, int nchunk, long long ld,
+                            long long ncol, double factor, double *__restrict__ out) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncol) return;
+  double v = 0.0;
+  for (int k = 0; k < nchunk; ++k) v += part[(long long)k * ld + c];
+  out[c] = factor * v;
+}
+
+// out[n][r] = factor * rowscale[r] * modscale[n] * sum_s P[s][n][r]
+// (FP64 reduction of split-K partials; either scale may be absent)
+__global__ void k_splitk_reduce(const float *__restrict__ P, int nsplit, long long slice,
+                                int nmod, int nrow, long long ldp, const float *__restrict__ rowscale,
+                                const float *__restrict__ modscale,
+                                const double *__restrict__ modmean,
+                                const double *__restrict__ rowsum, double factor,
+                                double *__restrict__ out, long long ld_out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nmod * nrow) return;
+  const int n = t / nrow, r = t % nrow;
+  const float *p = P + (long long)n * ldp + r;
+  // independent partial sums keep several loads in flight
+  double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+  int s = 0;
+  for (; s + 3 < nsplit; s += 4) {
+    v0 += (double)p[(long long)s * slice];
+    v1 += (double)p[(long long)(s + 1) * slice];
+    v2 += (double)p[(long long)(s + 2) * slice];
+    v3 += (double)p[(long long)(s + 3) * slice];
+  }
+  for (; s < nsplit; ++s) v0 += (double)p[(long long)s * slice];
+  double v = (v0 + v1) + (v2 + v3);
+  if (rowscale) v *= (double)rowscale[r];
+  if (modscale) v *= (double)modscale[n];
+  if (modmean) v += modmean[n] * rowsum[r];  // the model mean removed before the product
+  out[(long long)n * ld_out + r] = factor * v;
+}
+
+// Per (station, model): stored-row sums -> raw data (+ background) -> transform.
+// sums [nmod][ld_sums] with row s*NS + q; models [nmod][ld_models] (background
+// values at column ngrid); data [nmod][ld_data]; raw_out [nmod][nmeas*raw] optional.
+__global__ void k_stored_assemble(int kind, int transform, double tbx, double tby, double tbz,
+                                  int nmeas, int nmod, const double *__restrict__ sums,
+                                  long long ld_sums, const double *__restrict__ bgsens, int nbg,
+                                  const double *__restrict__ models, long long ld_models,
+                                  long long ngrid, MagField mf, double *__restrict__ raw_out,
+                                  double *__restrict__ data, long long ld_data) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nmeas * nmod) return;
+  const int n = t / nmeas, s = t % nmeas;
+  const int raw = kind_raw(kind);
+  const int ns = kind == KIND_MAGNETIC ? 3 : kind_ncomp(kind);
+  const double *sm = sums + n * ld_sums + (long long)s * ns;
+  double r[10];
+  if (kind == KIND_MAGNETIC) {
+    for (int c = 0; c < 3; ++c) r[c] = sm[c];
+  } else {
+    double u[NC_COUNT];
+    for (int c = 0; c < NC_COUNT; ++c) u[c] = 0.0;
+    for (int q = 0; q < ns; ++q) u[slot_comp(kind, q)] = sm[q];
+    raw_from_comps(kind, u, mf, r);
+  }
+  const double *bgval = models + n * ld_models + ngrid;
+  for (int c = 0; c < raw; ++c) {
+    double bg = 0.0;
+    for (int j = 0; j < nbg; ++j)
+      bg = add(bg, mul(bgsens[((long long)s * raw + c) * nbg + j], bgval[j]));
+    r[c] = add(r[c], bg);
+    if (raw_out) raw_out[n * (long long)nmeas * raw + (long long)s * raw + c] = r[c];
+  }
+  double *d = data + n * ld_data;
+  if (transform == TR_NONE) {
+    for (int c = 0; c < raw; ++c) d[(long long)s * raw + c] = r[c];
+  } else if (transform == TR_FTG_INVARIANT) {
+    d[s] = sub(sub(sub(add(add(mul(r[0], r[4]), mul(r[4], r[8])), mul(r[0], r[8])), mul(r[3], r[1])),
+                   mul(r[7], r[5])),
+               mul(r[2], r[6]));
+  } else if (transform == TR_TOTAL_FIELD) {
+    d[s] = sqrt(add(add(mul(r[0], r[0]), mul(r[1], r[1])), mul(r[2], r[2])));
+  } else {
+    d[s] = add(add(mul(tbx, r[0]), mul(tby, r[1])), mul(tbz, r[2]));
+  }
+}
+
+// Per (station, model): misfit -> raw weights (through the transform
+// derivative) -> stored-row weights.  w_raw [nmod][nmeas*raw], w_st [nmod][ld_w].
+__global__ void k_stored_weights(int kind, int transform, double tbx, double tby, double tbz,
+                                 int nmeas, int nmod, const double *__restrict__ misfit,
+                                 long long ld_misfit, const double *__restrict__ rawd, MagField mf,
+                                 double *__restrict__ w_raw, double *__restrict__ w_st,
+                                 long long ld_w) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nmeas * nmod) return;
+  const int n = t / nmeas, s = t % nmeas;
+  const int raw = kind_raw(kind);
+  const int ns = kind == KIND_MAGNETIC ? 3 : kind_ncomp(kind);
+  const double *mis = misfit + n * ld_misfit;
+  double w[10];
+  if (transform == TR_NONE) {
+    for (int c = 0; c < raw; ++c) w[c] = mis[(long long)s * raw + c];
+  } else {
+    const double m = mis[s];
+    const double *d = rawd + n * (long long)nmeas * raw + (long long)s * raw;
+    if (transform == TR_FTG_INVARIANT) {
+      w[0] = mul(m, add(d[4], d[8])); w[1] = mul(m, -d[3]); w[2] = mul(m, -d[6]);
+      w[3] = mul(m, -d[1]); w[4] = mul(m, add(d[0], d[8])); w[5] = mul(m, -d[7]);
+      w[6] = mul(m, -d[2]); w[7] = mul(m, -d[5]); w[8] = mul(m, add(d[0], d[4]));
+    } else if (transform == TR_TOTAL_FIELD) {
+      const double tt = sqrt(add(add(mul(d[0], d[0]), mul(d[1], d[1])), mul(d[2], d[2])));
+      for (int c = 0; c < 3; ++c) w[c] = mul(m, d[c] / tt);
+    } else {
+      w[0] = mul(m, tbx); w[1] = mul(m, tby); w[2] = mul(m, tbz);
+    }
+  }
+  double *wr = w_raw + n * (long long)nmeas * raw + (long long)s * raw;
+  for (int c = 0; c < raw; ++c) wr[c] = w[c];
+  double *ws = w_st + n * ld_w + (long long)s * ns;
+  if (kind == KIND_MAGNETIC) {
+    for (int c = 0; c < 3; ++c) ws[c] = w[c];
+  } else {
+    double u[NC_COUNT];
+    comps_from_raw_weights(kind, w, mf, u);
+    for (int q = 0; q < ns; ++q) ws[q] = u[slot_comp(kind, q)];
+  }
+}
+
+// grads[n][ngrid + j] = 2 sum_s sum_r w_raw[n][s][r] bgsens[s][r][j]; block (j, n)
+__global__ void k_bg_grad_batched(int raw, int nmeas, int nbg, const double *__restrict__ w_raw,
+                                  const double *__restrict__ bgsens, double *__restrict__ grads,
+                                  long long ld_grads, long long ngrid) {
+  const int j = blockIdx.x, n = blockIdx.y;
+  const double *w = w_raw + n * (long long)nmeas * raw;
+  double acc = 0.0;
+  for (int s = threadIdx.x; s < nmeas; s += kT)
+    for (int r = 0; r < raw; ++r)
+      acc = fma(w[(long long)s * raw + r], bgsens[((long long)s * raw + r) * nbg + j], acc);
+  __shared__ double red[kT / 32];
+  acc = block_sum_d<kT>(acc, red);
+  if (threadIdx.x == 0) grads[n * ld_grads + ngrid + j] = 2.0 * acc;
+}
+
+inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
+inline int grid_for(long long n) {
+  long long b = (n + kT - 1) / kT;
+  return (int)(b > 152 * 64 ? 152 * 64 : (b < 1 ? 1 : b));
+}
+
+}  // namespace
+
+cudaError_t launch_split_rows(const double *rows, long long ld_in, long long ncol, int nrows,
+                              void *hi, void *lo, long long ld_out, float *scale, double *rowsum,
+                              long long row0, cudaStream_t st) {
+  if (nrows == 0) return cudaSuccess;
+  k_split_rows<<<nrows, kT, 0, st>>>(rows, ld_in, ncol, static_cast<__half *>(hi),
+                                     static_cast<__half *>(lo), ld_out, scale, rowsum, row0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_transpose16(const void *in, long long ld_in, long long rows, long long cols,
+                               void *out, long long ld_out, cudaStream_t st) {
+  dim3 grid(cdiv(cols, 32), cdiv(ld_out, 32));
+  k_transpose16<<<grid, 256, 0, st>>>(static_cast<const uint16_t *>(in), ld_in, rows, cols,
+                                      static_cast<uint16_t *>(out), ld_out);
+  return cudaGetLastError();
+}
+
+long long split_matrix_work(int nrow_pad, long long ld_dst) {
+  return 2LL * nrow_pad * ((ld_dst + kChunk - 1) / kChunk);
+}
+
+cudaError_t launch_split_matrix(const double *src, long long ld_src, int nrow, long long ncol,
+                                const float *colscale, void *hi, void *lo, long long ld_dst,
+                                int nrow_pad, float *rowscale, double *rowmean, double *work,
+                                cudaStream_t st) {
+  if (nrow_pad == 0) return cudaSuccess;
+  const int nchunk = cdiv(ld_dst, kChunk);
+  double *pmax = work, *psum = work + (long long)nrow_pad * nchunk;
+  dim3 grid(nchunk, nrow_pad);
+  k_row_stats<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, pmax, psum, nchunk);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_row_finalize<<<cdiv(nrow_pad, 128), 128, 0, st>>>(nrow_pad, nchunk, ncol, rowmean != nullptr,
+                                                      pmax, psum, rowscale, rowmean);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_split_chunks<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, rowscale, rowmean,
+                                      static_cast<__half *>(hi), static_cast<__half *>(lo),
+                                      ld_dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_f32(const double *src, long long n, long long npad, float *dst,
+                          cudaStream_t st) {
+  k_to_f32<<<grid_for(npad), kT, 0, st>>>(src, n, npad, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gemv_f32(const float *J, long long ld, int nrows, const float *x, double *out,
+                            cudaStream_t st) {
+  if (nrows == 0) return cudaSuccess;
+  k_gemv_f32<<<nrows, kT, 0, st>>>(J, ld, x, out);
+  return cudaGetLastError();
+}
+
+int gemv_t_chunks(int nrows) { return cdiv(nrows, kRC); }
+
+cudaError_t launch_gemv_t_f32(const float *J, long long ld, int nrows, const double *w,
+                              double *part, long long ncol, double factor, double *out,
+                              cudaStream_t st) {
+  const int nchunk = gemv_t_chunks(nrows);
+  dim3 grid(cdiv(ld / 4, kT), nchunk);
+  k_gemv_t_f32<<<grid, kT, 0, st>>>(J, ld, nrows, w, part);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_sum_parts<<<cdiv(ncol, kT), kT, 0, st>>>(part, nchunk, ld, ncol, factor, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_splitk_reduce(const float *P, int nsplit, long long slice, int nmod, int nrow,
+                                 long long ldp, const float *rowscale, const float *modscale,
+                                 const double *modmean, const double *rowsum, double factor,
+                                 double *out, long long ld_out, cudaStream_t st) {
+  const long long n = (long long)nmod * nrow;
+  if (n == 0) return cudaSuccess;
+  k_splitk_reduce<<<cdiv(n, kT), kT, 0, st>>>(P, nsplit, slice, nmod, nrow, ldp, rowscale,
+                                               modscale, modmean, rowsum, factor, out, ld_out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stored_assemble(int kind, int transform, double tbx, double tby, double tbz,
+                                   int nmeas, int nmod, const double *sums, long long ld_sums,
+                                   const double *bgsens, int nbg, const double *models,
+                                   long long ld_models, long long ngrid, const MagField &mf,
+                                   double *raw_out, double *data, long long ld_data,
+                                   cudaStream_t st) {
+  const long long n = (long long)nmeas * nmod;
+  if (n == 0) return cudaSuccess;
+  k_stored_assemble<<<cdiv(n, 128), 128, 0, st>>>(kind, transform, tbx, tby, tbz, nmeas, nmod,
+                                                  sums, ld_sums, bgsens, nbg, models, ld_models,
+                                                  ngrid, mf, raw_out, data, ld_data);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stored_weights(int kind, int transform, double tbx, double tby, double tbz,
+                                  int nmeas, int nmod, const double *misfit, long long ld_misfit,
+                                  const double *rawd, const MagField &mf, double *w_raw,
+                                  double *w_st, long long ld_w, cudaStream_t st) {
+  const long long n = (long long)nmeas * nmod;
+  if (n == 0) return cudaSuccess;
+  k_stored_weights<<<cdiv(n, 128), 128, 0, st>>>(kind, transform, tbx, tby, tbz, nmeas, nmod,
+                                                 misfit, ld_misfit, rawd, mf, w_raw, w_st, ld_w);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bg_grad_batched(int raw, int nmeas, int nbg, int nmod, const double *w_raw,
+                                   const double *bgsens, double *grads, long long ld_grads,
+                                   long long ngrid, cudaStream_t st) {
+  if (nbg == 0 || nmod == 0) return cudaSuccess;
+  k_bg_grad_batched<<<dim3(nbg, nmod), kT, 0, st>>>(raw, nmeas, nbg, w_raw, bgsens, grads,
+                                                     ld_grads, ngrid);
+  return cudaGetLastError();
+}
+
+}  // namespace j3g

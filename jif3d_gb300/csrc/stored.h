@@ -1,0 +1,78 @@
+// stored.h -- device-resident sensitivity storage and its products (internal).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "kinds.h"
+
+namespace j3g {
+
+// fp16 hi / lo split of FP64 rows with a power-of-two row scale
+// (scale[row0 + r]): row = scale * (hi + lo), max|hi| in (2^13, 2^14].
+// rowsum (optional) receives the FP64 row sums J 1.
+cudaError_t launch_split_rows(const double *rows, long long ld_in, long long ncol, int nrows,
+                              void *hi, void *lo, long long ld_out, float *scale, double *rowsum,
+                              long long row0, cudaStream_t st);
+// out[c][r] = in[r][c] for r < rows (zero for rows <= r < ld_out), c < cols; 16-bit elements.
+cudaError_t launch_transpose16(const void *in, long long ld_in, long long rows, long long cols,
+                               void *out, long long ld_out, cudaStream_t st);
+// FP64 [nrow][ld_src] (column c times colscale[c] when given) -> fp16 hi / lo
+// [nrow_pad][ld_dst] with a power-of-two scale per row into rowscale[r]; rows
+// beyond nrow and columns beyond ncol are zero.
+// With rowmean given, each row is centred first (rowmean[r] = its mean over
+// the ncol columns).  work: split_matrix_work(nrow_pad, ld_dst) doubles.
+long long split_matrix_work(int nrow_pad, long long ld_dst);
+cudaError_t launch_split_matrix(const double *src, long long ld_src, int nrow, long long ncol,
+                                const float *colscale, void *hi, void *lo, long long ld_dst,
+                                int nrow_pad, float *rowscale, double *rowmean, double *work,
+                                cudaStream_t st);
+cudaError_t launch_to_f32(const double *src, long long n, long long npad, float *dst,
+                          cudaStream_t st);
+// d[r] = sum_c J[r][c] x[c] (FP32 J, FP32 x, FP64 result), ld multiple of 4.
+cudaError_t launch_gemv_f32(const float *J, long long ld, int nrows, const float *x, double *out,
+                            cudaStream_t st);
+// out[c] = factor * sum_r J[r][c] w[r]; part needs gemv_t_chunks(nrows) * ld doubles.
+int gemv_t_chunks(int nrows);
+cudaError_t launch_gemv_t_f32(const float *J, long long ld, int nrows, const double *w,
+                              double *part, long long ncol, double factor, double *out,
+                              cudaStream_t st);
+// out[n][r] = factor * rowscale[r] * modscale[n] * sum_s P[s][n][r]  (P float, out double)
+// + modmean[n] * rowsum[r] when modmean is given (adds back a centred mean).
+cudaError_t launch_splitk_reduce(const float *P, int nsplit, long long slice, int nmod, int nrow,
+                                 long long ldp, const float *rowscale, const float *modscale,
+                                 const double *modmean, const double *rowsum, double factor,
+                                 double *out, long long ld_out, cudaStream_t st);
+
+// Batched epilogues of the stored products (grid over station x model).
+cudaError_t launch_stored_assemble(int kind, int transform, double tbx, double tby, double tbz,
+                                   int nmeas, int nmod, const double *sums, long long ld_sums,
+                                   const double *bgsens, int nbg, const double *models,
+                                   long long ld_models, long long ngrid, const MagField &mf,
+                                   double *raw_out, double *data, long long ld_data,
+                                   cudaStream_t st);
+cudaError_t launch_stored_weights(int kind, int transform, double tbx, double tby, double tbz,
+                                  int nmeas, int nmod, const double *misfit, long long ld_misfit,
+                                  const double *rawd, const MagField &mf, double *w_raw,
+                                  double *w_st, long long ld_w, cudaStream_t st);
+cudaError_t launch_bg_grad_batched(int raw, int nmeas, int nbg, int nmod, const double *w_raw,
+                                   const double *bgsens, double *grads, long long ld_grads,
+                                   long long ngrid, cudaStream_t st);
+
+// Tensor-core products.  A [m][ld], B [n_pad][ld], K-major fp16 (or bf16), ld
+// a multiple of 64, n_pad a multiple of gemm_n_tile(n), 16-byte aligned bases.
+struct GemmOperands {
+  const void *a_hi, *a_lo;  // 16-bit elements: bf16, or fp16 when f16 is set
+  long long m;
+  const void *b_hi, *b_lo;
+  long long n, n_pad;
+  long long ld;
+  bool f16;
+};
+int gemm_n_tile(int n);
+int gemm_splits_used(long long ld, int nsplit);
+// P[split][n][ldp] (split stride `slice`) = per-split sums of
+// Ahi Bhi + Ahi Blo + Alo Bhi; err receives a non-zero code if a bounded
+// wait expired.
+cudaError_t launch_gemm_x3(const GemmOperands &g, int nsplit, float *P, long long ldp,
+                           long long slice, int *err, cudaStream_t st);
+
+}  // namespace j3g

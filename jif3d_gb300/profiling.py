@@ -2,6 +2,8 @@
 
     python -m jif3d_gb300.profiling node [--stations 64]   # node-term fwd + adjoint
     python -m jif3d_gb300.profiling fp64-weights           # libm FP64 weight probes
+    python -m jif3d_gb300.profiling gemm [--stations 128]  # tensor-core batched products
+    python -m jif3d_gb300.profiling stream [--stations 400] # FP32 streaming products
 
 Each case runs a few launches on a few-MB problem so that an ncu capture of
 it ends by itself.
@@ -27,6 +29,44 @@ def case_node(stations: int) -> None:
     ctx.close()
 
 
+def case_gemm(stations: int, models: int) -> None:
+    """Tensor-core batched products on the config-4 mesh with a station
+    subset: one batched forward and one batched adjoint (~0.5 GB of J)."""
+    from . import capi, workloads as W
+    s = W.config4(nmodels=models)
+    step = max(1, s.stations.shape[0] // stations)
+    s = s.subset(np.arange(0, s.stations.shape[0], step)[:stations])
+    ctx = capi.Context(0)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    d = ctx.batched_forward(s.models)
+    g = ctx.batched_lqderivative(s.models, np.ones_like(d))
+    print("gemm case ok", s.stations.shape[0], "stations", models, "models", float(d[0, 0]),
+          float(g[0, 0]))
+    ctx.close()
+
+
+def case_stream(stations: int) -> None:
+    """FP32 streaming products on the config-2 mesh with a station subset."""
+    import torch
+    from . import capi, workloads as W
+    s = W.config2()
+    step = max(1, s.stations.shape[0] // stations)
+    s = s.subset(np.arange(0, s.stations.shape[0], step)[:stations])
+    ctx = capi.Context(0)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(capi.STORE_FP32)
+    n = s.stations.shape[0]
+    dm = torch.tensor(s.model, dtype=torch.float64, device="cuda")
+    dd = torch.zeros(n * 9, dtype=torch.float64, device="cuda")
+    dg = torch.zeros(s.nparm, dtype=torch.float64, device="cuda")
+    ctx.stored_forward_device(dm.data_ptr(), dd.data_ptr())
+    ctx.stored_lqderivative_device(dm.data_ptr(), dd.data_ptr(), dg.data_ptr())
+    ctx.synchronize()
+    print("stream case ok", n, "stations", float(dd[0]), float(dg[0]))
+    ctx.close()
+
+
 def case_fp64_weights(n_iter: int) -> None:
     from . import capi
     lib = capi.load()
@@ -43,9 +83,18 @@ def main(argv=None) -> None:
     n.add_argument("--stations", type=int, default=64)
     w = sub.add_parser("fp64-weights")
     w.add_argument("--iters", type=int, default=1000)
+    g = sub.add_parser("gemm")
+    g.add_argument("--stations", type=int, default=128)
+    g.add_argument("--models", type=int, default=256)
+    st = sub.add_parser("stream")
+    st.add_argument("--stations", type=int, default=400)
     a = p.parse_args(argv)
     if a.case == "node":
         case_node(a.stations)
+    elif a.case == "gemm":
+        case_gemm(a.stations, a.models)
+    elif a.case == "stream":
+        case_stream(a.stations)
     elif a.case == "fp64-weights":
         case_fp64_weights(a.iters)
 

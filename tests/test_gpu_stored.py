@@ -1,0 +1,167 @@
+"""GPU parity of the stored-sensitivity (mixed precision) paths.
+
+Tolerance (mixed path): relative norm error <= 1e-6 per output group against
+the FP64 oracle, the bound stated for the mixed-precision path.  J is stored
+in FP32 (streaming products) or as fp16 hi + lo with a power-of-two row
+scale (tensor-core products); the FP64 matrix-free path serves as the
+reference at full sizes (its own parity with the oracle is <= 1e-10).
+"""
+import numpy as np
+import pytest
+
+from helpers import oracle_forward, oracle_lqderivative, relerr, small_survey
+from jif3d_gb300 import capi, workloads as W
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-6
+
+
+def groups(s, v):
+    """Split a data vector into the output groups of its kind (joint: g_z, tensor)."""
+    v = np.asarray(v)
+    if s.kind == W.JOINT and s.transform == W.T_NONE:
+        r = v.reshape(-1, 10)
+        return [r[:, 0], r[:, 1:]]
+    return [v]
+
+
+def check_groups(s, got, ref, tol=TOL):
+    for g, r in zip(groups(s, got), groups(s, ref)):
+        e = relerr(g, r)
+        assert e <= tol, e
+
+
+def dev(a):
+    import torch
+    return torch.tensor(np.ascontiguousarray(a), dtype=torch.float64, device="cuda")
+
+
+@pytest.mark.parametrize("storage", [capi.STORE_FP32, capi.STORE_F16X2])
+@pytest.mark.parametrize("kind", [W.SCALAR, W.TENSOR, W.MAGNETIC, W.JOINT])
+def test_stored_single_model(ctx, oracle_lib, storage, kind):
+    import torch
+    s = small_survey(kind, seed=200 + kind, nx=9, ny=8, nz=6, nmeas=12)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(storage)
+    info = ctx.sensitivity_info()
+    assert info["storage"] == storage and info["cols"] == s.ngrid
+    n = s.stations.shape[0]
+    d = torch.zeros(n * s.dpm, dtype=torch.float64, device="cuda")
+    ctx.stored_forward_device(dev(s.model).data_ptr(), d.data_ptr())
+    ctx.synchronize()
+    check_groups(s, d.cpu().numpy(), oracle_forward(oracle_lib, s))
+    misfit = np.random.default_rng(kind).normal(size=n * s.dpm)
+    g = torch.zeros(s.nparm, dtype=torch.float64, device="cuda")
+    dm, dr = dev(s.model), dev(misfit)
+    ctx.stored_lqderivative_device(dm.data_ptr(), dr.data_ptr(), g.data_ptr())
+    ctx.synchronize()
+    gref = oracle_lqderivative(oracle_lib, s, misfit)
+    assert relerr(g.cpu().numpy(), gref) <= TOL
+
+
+@pytest.mark.parametrize("kind,transform", [(W.TENSOR, W.T_FTG_INVARIANT),
+                                            (W.MAGNETIC, W.T_TOTAL_FIELD),
+                                            (W.MAGNETIC, W.T_TFA)])
+def test_batched_transforms(ctx, oracle_lib, kind, transform):
+    s = small_survey(kind, seed=230 + transform, transform=transform, nx=8, ny=7, nz=5)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    rng = np.random.default_rng(3)
+    models = s.model[None, :] * (1 + 0.1 * rng.normal(size=(3, s.nparm)))
+    d = ctx.batched_forward(models)
+    n = s.stations.shape[0]
+    mis = rng.normal(size=(3, n))
+    g = ctx.batched_lqderivative(models, mis)
+    for i in range(3):
+        assert relerr(d[i], oracle_forward(oracle_lib, s, models[i])) <= TOL
+        assert relerr(g[i], oracle_lqderivative(oracle_lib, s, mis[i], models[i])) <= TOL
+
+
+@pytest.mark.parametrize("nmodels", [1, 5, 70, 130])
+def test_batched_joint_many_models(ctx, oracle_lib, nmodels):
+    """Batched products for N-tile sizes 64 / 128 / 256 against the oracle on
+    a few models and against the single-model stored product on all."""
+    import torch
+    s = small_survey(W.JOINT, seed=250, nx=12, ny=10, nz=7, nmeas=15)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    rng = np.random.default_rng(nmodels)
+    models = s.model[None, :] + 2.0 * rng.normal(size=(nmodels, s.nparm))
+    n = s.stations.shape[0]
+    d = ctx.batched_forward(models)
+    mis = rng.normal(size=(nmodels, n * 10))
+    g = ctx.batched_lqderivative(models, mis)
+    for i in sorted({0, nmodels // 2, nmodels - 1}):
+        check_groups(s, d[i], oracle_forward(oracle_lib, s, models[i]))
+        assert relerr(g[i], oracle_lqderivative(oracle_lib, s, mis[i], models[i])) <= TOL
+
+
+def test_stored_is_dropped_on_new_geometry(ctx):
+    s = small_survey(W.SCALAR, seed=5)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(capi.STORE_FP32)
+    assert ctx.sensitivity_info()["storage"] == capi.STORE_FP32
+    ctx.set_stations(s.stations[:, 0] + 1.0, s.stations[:, 1], s.stations[:, 2])
+    assert ctx.sensitivity_info()["storage"] == 0
+    with pytest.raises(capi.J3GError):
+        ctx.batched_forward(s.model[None, :])
+
+
+def test_config2_fp32_stored_full(ctx):
+    """Config 2 at full size (FP32 J, 5 GB): stored forward and adjoint
+    against the FP64 matrix-free path."""
+    import torch
+    s = W.config2()
+    W.setup_context(ctx, s)
+    n = s.stations.shape[0]
+    dm = dev(s.model)
+    ref = torch.zeros(n * 9, dtype=torch.float64, device="cuda")
+    ctx.forward_device(dm.data_ptr(), ref.data_ptr())
+    mis = dev(np.random.default_rng(2).normal(size=n * 9))
+    gref = torch.zeros(s.nparm, dtype=torch.float64, device="cuda")
+    ctx.lqderivative_device(dm.data_ptr(), mis.data_ptr(), gref.data_ptr())
+    ctx.synchronize()
+    ctx.build_sensitivity(capi.STORE_FP32)
+    d = torch.zeros_like(ref)
+    g = torch.zeros_like(gref)
+    ctx.stored_forward_device(dm.data_ptr(), d.data_ptr())
+    ctx.stored_lqderivative_device(dm.data_ptr(), mis.data_ptr(), g.data_ptr())
+    ctx.synchronize()
+    assert relerr(d.cpu().numpy(), ref.cpu().numpy()) <= TOL
+    assert relerr(g.cpu().numpy(), gref.cpu().numpy()) <= TOL
+    ctx.drop_sensitivity()
+
+
+def test_config4_batched_full(ctx, oracle_lib):
+    """Config 4 at full size: 256 models through the tensor-core products;
+    four of them checked against the FP64 matrix-free path, one station
+    subset against the oracle."""
+    import torch
+    s = W.config4()
+    W.setup_context(ctx, s)
+    n = s.stations.shape[0]
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    models = dev(s.models)
+    data = torch.zeros((256, n * 10), dtype=torch.float64, device="cuda")
+    ctx.batched_forward_device(256, models.data_ptr(), data.data_ptr())
+    rng = np.random.default_rng(4)
+    mis_h = rng.normal(size=(256, n * 10)) * np.tile([1e8] + [1e9] * 9, n)
+    mis = dev(mis_h)
+    grads = torch.zeros_like(models)
+    ctx.batched_lqderivative_device(256, models.data_ptr(), mis.data_ptr(), grads.data_ptr())
+    ctx.synchronize()
+    data_h, grads_h = data.cpu().numpy(), grads.cpu().numpy()
+    ctx.drop_sensitivity()
+    for i in (0, 77, 255):
+        ref = torch.zeros(n * 10, dtype=torch.float64, device="cuda")
+        gref = torch.zeros(s.nparm, dtype=torch.float64, device="cuda")
+        ctx.forward_device(models[i].data_ptr(), ref.data_ptr())
+        ctx.lqderivative_device(models[i].data_ptr(), mis[i].contiguous().data_ptr(),
+                                gref.data_ptr())
+        ctx.synchronize()
+        check_groups(s, data_h[i], ref.cpu().numpy())
+        assert relerr(grads_h[i], gref.cpu().numpy()) <= TOL
+    sub = s.subset(np.arange(0, n, 128))
+    idx = np.arange(0, n, 128)
+    dsub = data_h[5].reshape(n, 10)[idx].ravel()
+    check_groups(sub, dsub, oracle_forward(oracle_lib, sub, s.models[5]))
