@@ -9,13 +9,14 @@
 //
 // Accuracy.  The tensor core's FP32 accumulation loses about 2e-8 relative
 // per MMA step, growing linearly with the number of steps that feed one
-// accumulator.  So the hi*hi products of every kStepsPerDrain MMA steps (32
-// cells) go to a fresh TMEM accumulator (double-buffered, A0 / A1) that the
-// drain warps add, with round-to-nearest FP32 adds, into sums held in
-// registers while the next steps are multiplied; the cross terms hi*lo +
-// lo*hi, about 2^-11 of the total, accumulate in a third TMEM region (X) for
-// the whole split.  Splits of at most 64 k-blocks keep the register sums
-// short; the caller adds the splits in FP64.
+// accumulator.  So every kStepsPerDrain 16-wide steps (32 cells) go to a
+// fresh TMEM accumulator -- first the cross terms hi*lo + lo*hi (about 2^-11
+// of the total), then the hi*hi products, so the large terms meet an
+// accumulator of their own size -- and the drain warps add it, with
+// round-to-nearest FP32 adds, into sums held in registers while the next
+// steps are multiplied into the other accumulators (four in rotation).
+// Splits of at most 64 k-blocks keep the register sums short; the caller adds
+// the splits in FP64.
 //
 // One CTA computes a 128 x BN tile of one K split with 10 warps:
 //   warp 0      TMA producer (Ahi, Alo, Bhi, Blo per stage, 128-byte swizzle)
@@ -43,6 +44,7 @@ constexpr int kDrainWarps = 8;
 // drained into the register sums; 2 halves the tensor-core rounding of 4
 constexpr int kStepsPerDrain = 2;
 constexpr int kDrainsPerBlock = (BK / 16) / kStepsPerDrain;
+constexpr int kAccBufs = 4;  // TMEM accumulators in rotation (4 x BN columns)
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 
 template <int BN, bool F16> struct Cfg {
@@ -50,9 +52,9 @@ template <int BN, bool F16> struct Cfg {
   static constexpr int A_BYTES = BM * BK * 2;
   static constexpr int B_BYTES = BN * BK * 2;
   static constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;
-  static constexpr int NBAR = 2 * STAGES + 5;  // full, empty, A full x2, A empty x2, X full
+  static constexpr int NBAR = 2 * STAGES + 2 * kAccBufs;  // stage full / empty, buffer full / empty
   static constexpr int SMEM = STAGES * STAGE_BYTES + NBAR * 8 + 16 + 1024;
-  static constexpr uint32_t TMEM_COLS = 4 * BN;  // A0, A1, X (+ unused), power of two
+  static constexpr uint32_t TMEM_COLS = kAccBufs * BN;  // accumulator buffers, power of two
   // kind::f16 instruction descriptor: D F32 (bit 4), A and B format at bits
   // 7 and 10 (0 = F16, 1 = BF16), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
   static constexpr uint32_t FMT = F16 ? 0u : 1u;
@@ -172,21 +174,21 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
                                               ~static_cast<uintptr_t>(1023));
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * C::STAGE_BYTES);
   uint64_t *full = bars, *empty = bars + S;
-  uint64_t *a_full = bars + 2 * S, *a_empty = bars + 2 * S + 2, *x_full = bars + 2 * S + 4;
+  uint64_t *a_full = bars + 2 * S, *a_empty = bars + 2 * S + kAccBufs;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + C::NBAR);
   volatile int *fail = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;  // N tiles fastest (see launch_bn)
   const int kb0 = blockIdx.z * kb_per_split;
   const int nkb = min(kb_total, kb0 + kb_per_split) - kb0;
+  const int ndrain = nkb * kDrainsPerBlock;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < 2 * S; ++s) mbar_init(smem_u32(bars + s), 1);
-    mbar_init(smem_u32(a_full), 1);
-    mbar_init(smem_u32(a_full + 1), 1);
-    mbar_init(smem_u32(a_empty), kDrainWarps);
-    mbar_init(smem_u32(a_empty + 1), kDrainWarps);
-    mbar_init(smem_u32(x_full), 1);
+    for (int b = 0; b < kAccBufs; ++b) {
+      mbar_init(smem_u32(a_full + b), 1);
+      mbar_init(smem_u32(a_empty + b), kDrainWarps);
+    }
     *fail = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tmAhi)) : "memory");
@@ -205,8 +207,6 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t tmemA[2] = {tmem, tmem + (uint32_t)BN};
-  const uint32_t tmemX = tmem + 2u * BN;
 
   if (warp == 0) {
     // ---------------- TMA producer ----------------
@@ -237,6 +237,10 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
+    // Drain d covers kStepsPerDrain 16-wide steps of one k-block and goes to
+    // accumulator buffer d % kAccBufs: first the small cross terms (the
+    // buffer starts from zero), then the hi*hi products, so that the large
+    // terms are added last to an accumulator of their own size.
     if (lane == 0) {
       bool ok = true;
       for (int i = 0; i < nkb && ok; ++i) {
@@ -251,34 +255,35 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         const uint32_t ahi = base, alo = base + C::A_BYTES;
         const uint32_t bhi = base + 2 * C::A_BYTES, blo = bhi + C::B_BYTES;
 #pragma unroll
-        for (int kk = 0; kk < BK / 16; ++kk) {
-          const int d = i * kDrainsPerBlock + kk / kStepsPerDrain;  // drain index
-          const int b = d & 1;
-          if (kk % kStepsPerDrain == 0 && d >= 2 &&
-              !mbar_wait(smem_u32(a_empty + b), ((uint32_t)(d >> 1) & 1u) ^ 1u)) {
-            // the buffer of drain d-2 was never emptied
+        for (int j = 0; j < kDrainsPerBlock; ++j) {
+          const int d = i * kDrainsPerBlock + j;
+          const int b = d % kAccBufs;
+          if (d >= kAccBufs &&
+              !mbar_wait(smem_u32(a_empty + b), ((uint32_t)(d / kAccBufs) & 1u) ^ 1u)) {
+            // the buffer of drain d - kAccBufs was never emptied
             atomicExch(err, 3);
             ok = false;
             break;
           }
-          if (kk % kStepsPerDrain == 0) tc_fence_after();
-          const uint32_t off = kk * 32;  // 16 elements = 32 bytes along K inside the swizzle atom
-          const uint64_t dah = sw128_desc(ahi + off), dal = sw128_desc(alo + off);
-          const uint64_t dbh = sw128_desc(bhi + off), dbl = sw128_desc(blo + off);
-          umma(tmemA[b], dah, dbh, C::IDESC, (kk % kStepsPerDrain) > 0 ? 1u : 0u);
-          umma(tmemX, dah, dbl, C::IDESC, (i > 0 || kk > 0) ? 1u : 0u);
-          umma(tmemX, dal, dbh, C::IDESC, 1u);
-          if ((kk + 1) % kStepsPerDrain == 0)
-            umma_commit(smem_u32(a_full + b));  // this drain's hi*hi ready
+          tc_fence_after();
+          const uint32_t acc = tmem + (uint32_t)(b * BN);
+#pragma unroll
+          for (int t = 0; t < kStepsPerDrain; ++t) {
+            const uint32_t off = (j * kStepsPerDrain + t) * 32;  // 16 elements = 32 bytes
+            umma(acc, sw128_desc(ahi + off), sw128_desc(blo + off), C::IDESC, t > 0 ? 1u : 0u);
+            umma(acc, sw128_desc(alo + off), sw128_desc(bhi + off), C::IDESC, 1u);
+          }
+#pragma unroll
+          for (int t = 0; t < kStepsPerDrain; ++t) {
+            const uint32_t off = (j * kStepsPerDrain + t) * 32;
+            umma(acc, sw128_desc(ahi + off), sw128_desc(bhi + off), C::IDESC, 1u);
+          }
+          umma_commit(smem_u32(a_full + b));  // this drain's products are ready
         }
         if (!ok) break;
         umma_commit(smem_u32(empty + s));  // smem stage free once these MMAs finish
       }
-      if (ok) {
-        umma_commit(smem_u32(x_full));  // cross terms complete
-      } else {
-        *fail = 1;
-      }
+      if (!ok) *fail = 1;
     }
   } else {
     // ---------------- drain warps ----------------
@@ -286,47 +291,29 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     const int ch = (warp - 2) >> 2;                           // column half
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
     const uint32_t col0 = (uint32_t)(ch * C::COLS_PER_WARP);
-    float s[C::COLS_PER_WARP];  // round-to-nearest FP32 sums of the drained k-blocks
+    float s[C::COLS_PER_WARP];  // round-to-nearest FP32 sums of the drained accumulators
 #pragma unroll
     for (int j = 0; j < C::COLS_PER_WARP; ++j) s[j] = 0.0f;
-    bool ok = true;
-    for (int i = 0; i < nkb * kDrainsPerBlock; ++i) {  // i = drain index
-      const int b = i & 1;
-      bool got = mbar_wait(smem_u32(a_full + b), (uint32_t)(i >> 1) & 1u);
+    for (int d = 0; d < ndrain; ++d) {
+      const int b = d % kAccBufs;
+      bool got = mbar_wait(smem_u32(a_full + b), (uint32_t)(d / kAccBufs) & 1u);
       got = __all_sync(0xffffffffu, got ? 1 : 0) != 0;
       if (!got) {
         if (lane == 0) atomicExch(err, 4);
-        ok = false;
         break;
       }
       tc_fence_after();
+      const uint32_t acc = tmem + (uint32_t)(b * BN) + lane_off + col0;
 #pragma unroll
       for (int h = 0; h < C::COLS_PER_WARP / 16; ++h) {
         uint32_t v[16];
-        tmem_ld16(tmemA[b] + lane_off + col0 + 16u * h, v);
+        tmem_ld16(acc + 16u * h, v);
 #pragma unroll
         for (int j = 0; j < 16; ++j) s[16 * h + j] = __fadd_rn(s[16 * h + j], __uint_as_float(v[j]));
       }
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(smem_u32(a_empty + b));
-    }
-    if (ok) {
-      bool got = nkb > 0 && mbar_wait(smem_u32(x_full), 0u);
-      got = __all_sync(0xffffffffu, got ? 1 : 0) != 0;
-      if (got) {
-        tc_fence_after();
-#pragma unroll
-        for (int h = 0; h < C::COLS_PER_WARP / 16; ++h) {
-          uint32_t v[16];
-          tmem_ld16(tmemX + lane_off + col0 + 16u * h, v);
-#pragma unroll
-          for (int j = 0; j < 16; ++j)
-            s[16 * h + j] = __fadd_rn(s[16 * h + j], __uint_as_float(v[j]));
-        }
-      } else if (nkb > 0) {
-        if (lane == 0) atomicExch(err, 5);
-      }
     }
     const int row = m0 + q * 32 + lane;
     float *out = P + (long long)blockIdx.z * slice;
