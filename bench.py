@@ -209,6 +209,10 @@ def run_batched(args, rank, world, local):
     launches = ctx.launch_count() - l0
     gf_ms, gf_n = ctx.get_timing(capi.TIMER_GEMM_FORWARD)
     ga_ms, ga_n = ctx.get_timing(capi.TIMER_GEMM_ADJOINT)
+    phase_ms = {name: ctx.get_timing(t)[0] / args.steps
+                for name, t in (("split", capi.TIMER_SPLIT), ("split_sums", capi.TIMER_REDUCE),
+                                ("epilogue", capi.TIMER_EPILOGUE))}
+    phase_ms["gemm"] = (gf_ms + ga_ms) / args.steps
     ctx.set_timing(False)
     ctx.synchronize()
     clk = clocks.stop()
@@ -297,6 +301,7 @@ def run_batched(args, rank, world, local):
         "plain_fp64": {"value": plain_value, "unit": UNIT, "ms_per_step": plain_ms,
                        "what": "FP64 matrix-free fwd+adjoint of one model, same survey"},
         "speedup_vs_plain_fp64": value / plain_value,
+        "ms_per_step_by_phase": phase_ms,
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "clocks": clk,
     }
 

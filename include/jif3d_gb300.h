@@ -181,7 +181,10 @@ enum j3g_timer {
   J3G_TIMER_STREAM_FORWARD = 2, /* FP32 J m streaming product */
   J3G_TIMER_STREAM_ADJOINT = 3, /* FP32 J^T r streaming product (column blocks) */
   J3G_TIMER_GEMM_FORWARD = 4,   /* tensor-core J M */
-  J3G_TIMER_GEMM_ADJOINT = 5    /* tensor-core J^T R */
+  J3G_TIMER_GEMM_ADJOINT = 5,   /* tensor-core J^T R */
+  J3G_TIMER_SPLIT = 6,          /* fp16 hi / lo split of models and residual weights */
+  J3G_TIMER_REDUCE = 7,         /* FP64 sums of the per-split tensor-core partials */
+  J3G_TIMER_EPILOGUE = 8        /* batched data assembly, residual weights, background */
 };
 int j3g_set_timing(j3g_context *ctx, int enable);
 int j3g_get_timing(j3g_context *ctx, int category, double *total_ms, long long *launches);

@@ -18,7 +18,7 @@ SCALAR, TENSOR, MAGNETIC, JOINT = 1, 2, 3, 4
 T_NONE, T_FTG_INVARIANT, T_TOTAL_FIELD, T_TFA = 0, 1, 2, 3
 STORE_FP32, STORE_F16X2 = 1, 2
 (TIMER_NODE_FORWARD, TIMER_NODE_ADJOINT, TIMER_STREAM_FORWARD, TIMER_STREAM_ADJOINT,
- TIMER_GEMM_FORWARD, TIMER_GEMM_ADJOINT) = range(6)
+ TIMER_GEMM_FORWARD, TIMER_GEMM_ADJOINT, TIMER_SPLIT, TIMER_REDUCE, TIMER_EPILOGUE) = range(9)
 
 _P = ctypes.POINTER(ctypes.c_double)
 _VP = ctypes.c_void_p

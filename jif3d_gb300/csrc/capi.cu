@@ -595,10 +595,13 @@ int batched_forward_impl(j3g_context *c, int nmod, const double *d_models, doubl
     // models are centred (m - mean over cells); mean * (J 1) is added back in
     // FP64 after the product, so a large uniform part of a model -- whose
     // tensor response is nearly zero -- does not eat into the FP32 accuracy
-    J3G_LAUNCH(c, launch_split_matrix(d_models, np, nmod, K, nullptr, c->Bhi.p, c->Blo.p, ldK,
-                                      (int)npad, ptr<float>(c->mscale), ptr<double>(c->mmean),
-                                      ptr<double>(c->swork), c->stream));
-    c->launches += 2;  // statistics, finalise and split passes
+    {
+      TimedScope ts(c, J3G_TIMER_SPLIT);
+      J3G_LAUNCH(c, launch_split_matrix(d_models, np, nmod, K, nullptr, c->Bhi.p, c->Blo.p, ldK,
+                                        (int)npad, ptr<float>(c->mscale), ptr<double>(c->mmean),
+                                        ptr<double>(c->swork), c->stream));
+      c->launches += 2;  // statistics, finalise and split passes
+    }
     const int nsplit = choose_splits(R, (int)(npad / tile), ldK);
     const int nsp = gemm_splits_used(ldK, nsplit);
     const long long slice = (long long)nmod * R;
@@ -610,11 +613,13 @@ int batched_forward_impl(j3g_context *c, int nmod, const double *d_models, doubl
       J3G_LAUNCH(c, launch_gemm_x3(g, nsplit, ptr<float>(c->P), R, slice, ptr<int>(c->gerr),
                                    c->stream));
     }
+    TimedScope ts(c, J3G_TIMER_REDUCE);
     J3G_LAUNCH(c, launch_splitk_reduce(ptr<float>(c->P), nsp, slice, nmod, (int)R, R,
                                        ptr<float>(c->rowscale), ptr<float>(c->mscale),
                                        ptr<double>(c->mmean), ptr<double>(c->Jrowsum), 1.0,
                                        ptr<double>(c->sums), R, c->stream));
   }
+  TimedScope ts(c, J3G_TIMER_EPILOGUE);
   J3G_LAUNCH(c, launch_stored_assemble(c->kind, c->transform, tbx, tby, tbz, c->nmeas, nmod,
                                        ptr<double>(c->sums), R, nbg ? ptr<double>(c->bgsens) : nullptr,
                                        nbg, d_models, np, K, mag_field(c), raw_out, d_data,
@@ -638,9 +643,13 @@ int batched_adjoint_impl(j3g_context *c, int nmod, const double *d_models,
   }
   J3G_TRY(ensure(c, c->wrawb, sizeof(double) * (size_t)nmod * c->nmeas * raw));
   J3G_TRY(ensure(c, c->wst, sizeof(double) * (size_t)nmod * R));
-  J3G_LAUNCH(c, launch_stored_weights(c->kind, c->transform, tbx, tby, tbz, c->nmeas, nmod,
-                                      d_misfits, (long long)c->nmeas * c->dpm(), rawd, mag_field(c),
-                                      ptr<double>(c->wrawb), ptr<double>(c->wst), R, c->stream));
+  {
+    TimedScope ts(c, J3G_TIMER_EPILOGUE);
+    J3G_LAUNCH(c, launch_stored_weights(c->kind, c->transform, tbx, tby, tbz, c->nmeas, nmod,
+                                        d_misfits, (long long)c->nmeas * c->dpm(), rawd,
+                                        mag_field(c), ptr<double>(c->wrawb), ptr<double>(c->wst),
+                                        R, c->stream));
+  }
   if (c->storage == J3G_STORE_FP32) {
     J3G_TRY(ensure(c, c->part, sizeof(double) * (size_t)gemv_t_chunks((int)R) * ldK));
     for (int n = 0; n < nmod; ++n) {
@@ -657,10 +666,13 @@ int batched_adjoint_impl(j3g_context *c, int nmod, const double *d_models,
     J3G_TRY(ensure(c, c->mscale, sizeof(float) * (size_t)npad));
     J3G_TRY(ensure(c, c->swork, sizeof(double) * (size_t)split_matrix_work((int)npad, ldR)));
     // residual weights carry the row scale of J: J = s_r (hi + lo)
-    J3G_LAUNCH(c, launch_split_matrix(ptr<double>(c->wst), R, nmod, R, ptr<float>(c->rowscale),
-                                      c->Bhi.p, c->Blo.p, ldR, (int)npad, ptr<float>(c->mscale),
-                                      nullptr, ptr<double>(c->swork), c->stream));
-    c->launches += 2;  // statistics, finalise and split passes
+    {
+      TimedScope ts(c, J3G_TIMER_SPLIT);
+      J3G_LAUNCH(c, launch_split_matrix(ptr<double>(c->wst), R, nmod, R, ptr<float>(c->rowscale),
+                                        c->Bhi.p, c->Blo.p, ldR, (int)npad, ptr<float>(c->mscale),
+                                        nullptr, ptr<double>(c->swork), c->stream));
+      c->launches += 2;  // statistics, finalise and split passes
+    }
     const int nsplit = choose_splits(K, (int)(npad / tile), ldR);
     const int nsp = gemm_splits_used(ldR, nsplit);
     const long long slice = (long long)nmod * K;
@@ -672,13 +684,16 @@ int batched_adjoint_impl(j3g_context *c, int nmod, const double *d_models,
       J3G_LAUNCH(c, launch_gemm_x3(g, nsplit, ptr<float>(c->P), K, slice, ptr<int>(c->gerr),
                                    c->stream));
     }
+    TimedScope ts(c, J3G_TIMER_REDUCE);
     J3G_LAUNCH(c, launch_splitk_reduce(ptr<float>(c->P), nsp, slice, nmod, (int)K, K, nullptr,
                                        ptr<float>(c->mscale), nullptr, nullptr, 2.0, d_grads, np,
                                        c->stream));
   }
-  if (nbg)
+  if (nbg) {
+    TimedScope ts(c, J3G_TIMER_EPILOGUE);
     J3G_LAUNCH(c, launch_bg_grad_batched(raw, c->nmeas, nbg, nmod, ptr<double>(c->wrawb),
                                          ptr<double>(c->bgsens), d_grads, np, K, c->stream));
+  }
   return J3G_OK;
 }
 

@@ -16,8 +16,10 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdint>
 
+#include "fpbits.cuh"
 #include "stored.h"
 
 namespace j3g {
@@ -142,6 +144,8 @@ __global__ void k_transpose16(const uint16_t *__restrict__ in, long long ld_in, 
 //   k_split_chunks  per (row, column chunk): (v - mean) / scale -> hi + lo
 // v = src[r][c] * colscale[c] (colscale optional).
 constexpr int kChunk = 8192;
+constexpr int kBatch = 8;  // loads in flight per thread in the streaming passes
+static_assert(kChunk % (kT * kBatch) == 0, "chunk must be whole load batches");
 
 __device__ __forceinline__ double scaled_val(const double *src, long long ld_src, int nrow,
                                              long long ncol, const float *colscale, long long r,
@@ -156,13 +160,24 @@ __global__ void k_row_stats(const double *__restrict__ src, long long ld_src, in
                             double *__restrict__ part_max, double *__restrict__ part_sum,
                             int nchunk) {
   const long long r = blockIdx.y;
-  const long long c0 = (long long)blockIdx.x * kChunk;
-  double m = 0.0, sum = 0.0;
-  for (long long c = c0 + threadIdx.x; c < c0 + kChunk; c += kT) {
-    const double v = scaled_val(src, ld_src, nrow, ncol, colscale, r, c);
-    m = fmax(m, fabs(v));
-    sum += v;
+  const long long c0 = (long long)blockIdx.x * kChunk + threadIdx.x;
+  // The scale needs only the binade of max |v| (truncating the mantissa keeps
+  // it) and the centring mean only an estimate (the same value is added back
+  // after the product), so both run in FP32 on truncated values.
+  float mf = 0.0f, sf = 0.0f;
+  for (int j0 = 0; j0 < kChunk / kT; j0 += kBatch) {
+    double v[kBatch];  // a batch of independent loads in flight per thread
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u)
+      v[u] = scaled_val(src, ld_src, nrow, ncol, colscale, r, c0 + (long long)(j0 + u) * kT);
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const float a = approx_f32(v[u]);
+      mf = fmaxf(mf, fabsf(a));
+      sf += a;
+    }
   }
+  double m = (double)mf, sum = (double)sf;
   __shared__ double red[kT / 32];
   m = warp_max_d(m);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
@@ -200,17 +215,25 @@ __global__ void k_split_chunks(const double *__restrict__ src, long long ld_src,
                                const double *__restrict__ rowmean, __half *__restrict__ hi,
                                __half *__restrict__ lo, long long ld_dst) {
   const long long r = blockIdx.y;
-  const long long c0 = (long long)blockIdx.x * kChunk;
-  const double inv = 1.0 / (double)rowscale[r];
-  const double mean = rowmean ? rowmean[r] : 0.0;
-  for (long long c = c0 + threadIdx.x; c < c0 + kChunk && c < ld_dst; c += kT) {
-    const double v = (r < nrow && c < ncol)
-                         ? (scaled_val(src, ld_src, nrow, ncol, colscale, r, c) - mean) * inv
-                         : 0.0;
-    __half hv, lv;
-    split_half(v, hv, lv);
-    hi[r * ld_dst + c] = hv;
-    lo[r * ld_dst + c] = lv;
+  const long long c0 = (long long)blockIdx.x * kChunk + threadIdx.x;
+  const double inv = 1.0 / (double)rowscale[r];  // a power of two: exact
+  const double shift = rowmean ? -rowmean[r] * inv : 0.0;
+  for (int j0 = 0; j0 < kChunk / kT; j0 += kBatch) {
+    double v[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u)
+      v[u] = scaled_val(src, ld_src, nrow, ncol, colscale, r, c0 + (long long)(j0 + u) * kT);
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const long long c = c0 + (long long)(j0 + u) * kT;
+      if (c >= ld_dst) break;
+      // one FP64 operation per element, (v - mean) / scale; then FP32: the
+      // 24-bit float keeps more than the 22 bits that hi + lo carry
+      const float x = (r < nrow && c < ncol) ? f64_to_f32_ftz(fma(v[u], inv, shift)) : 0.0f;
+      const __half hv = __float2half_rn(x);
+      hi[r * ld_dst + c] = hv;
+      lo[r * ld_dst + c] = __float2half_rn(__fsub_rn(x, __half2float(hv)));
+    }
   }
 }
 
@@ -324,6 +347,57 @@ __global__ void k_splitk_reduce(const float *__restrict__ P, int nsplit, long lo
   if (modscale) v *= (double)modscale[n];
   if (modmean) v += modmean[n] * rowsum[r];  // the model mean removed before the product
   out[(long long)n * ld_out + r] = factor * v;
+}
+
+// The same over four consecutive rows per thread (nrow, ldp and slice multiples
+// of 4, P 16-byte aligned): float4 loads with kBatch splits in flight, and
+// the split sums accumulated as unevaluated FP32 pairs (hi + lo, error-free
+// two-sum), which carry about 48 bits -- as good as an FP64 sum of FP32
+// partials -- without the FP64 pipe.  Per output one FP64 add widens the pair;
+// the power-of-two scales are exponent adds.  factor is applied the same way
+// when it is a power of two (fpow2, 2^kfac), else by an FP64 multiply.
+__global__ void k_splitk_reduce4(const float *__restrict__ P, int nsplit, long long slice,
+                                 int nmod, int nrow, long long ldp,
+                                 const float *__restrict__ rowscale,
+                                 const float *__restrict__ modscale,
+                                 const double *__restrict__ modmean,
+                                 const double *__restrict__ rowsum, bool fpow2, int kfac,
+                                 double factor, double *__restrict__ out, long long ld_out) {
+  const int nq = nrow / 4;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)nmod * nq) return;
+  const int n = (int)(t / nq), r = (int)(t % nq) * 4;
+  const float4 *p = reinterpret_cast<const float4 *>(P + (long long)n * ldp + r);
+  const long long s4 = slice / 4;
+  float hi[4] = {0.0f, 0.0f, 0.0f, 0.0f}, lo[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  auto add4 = [&](const float4 &q) {
+    const float x[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      float sres, err;
+      two_sum(hi[i], x[i], sres, err);
+      hi[i] = sres;
+      lo[i] = __fadd_rn(lo[i], err);
+    }
+  };
+  int s = 0;
+  for (; s + kBatch <= nsplit; s += kBatch) {
+    float4 q[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) q[u] = __ldcs(p + (long long)(s + u) * s4);
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) add4(q[u]);
+  }
+  for (; s < nsplit; ++s) add4(__ldcs(p + (long long)s * s4));
+  const int kmod = (modscale ? pow2_exponent(modscale[n]) : 0) + (fpow2 ? kfac : 0);
+  double *o = out + (long long)n * ld_out + r;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    double v = f32_to_f64(hi[i]) + f32_to_f64(lo[i]);
+    v = scale_pow2(v, kmod + (rowscale ? pow2_exponent(rowscale[r + i]) : 0));
+    if (modmean) v = fma(modmean[n], fpow2 ? scale_pow2(rowsum[r + i], kfac) : rowsum[r + i], v);
+    o[i] = fpow2 ? v : factor * v;
+  }
 }
 
 // Per (station, model): stored-row sums -> raw data (+ background) -> transform.
@@ -512,6 +586,15 @@ cudaError_t launch_splitk_reduce(const float *P, int nsplit, long long slice, in
                                  double *out, long long ld_out, cudaStream_t st) {
   const long long n = (long long)nmod * nrow;
   if (n == 0) return cudaSuccess;
+  if (nrow % 4 == 0 && ldp % 4 == 0 && slice % 4 == 0 &&
+      (reinterpret_cast<uintptr_t>(P) & 15) == 0) {
+    int kf = 0;
+    const bool fpow2 = factor != 0.0 && std::frexp(factor, &kf) == 0.5;  // factor = 2^(kf-1)
+    k_splitk_reduce4<<<cdiv(n / 4, kT), kT, 0, st>>>(P, nsplit, slice, nmod, nrow, ldp, rowscale,
+                                                      modscale, modmean, rowsum, fpow2, kf - 1,
+                                                      factor, out, ld_out);
+    return cudaGetLastError();
+  }
   k_splitk_reduce<<<cdiv(n, kT), kT, 0, st>>>(P, nsplit, slice, nmod, nrow, ldp, rowscale,
                                                modscale, modmean, rowsum, factor, out, ld_out);
   return cudaGetLastError();
