@@ -280,7 +280,7 @@ def run_batched(args, rank, world, local):
     roof = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"],
             "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"], "traffic": None,
             "peak_source": f"{src} bf16_tflops (burst; fp16 MMA runs at the bf16 rate)",
-            "kernel": "k_gemm_x3<128, fp16> (3 fp16 products per launch)",
+            "kernel": "k_gemm_pair<fp16> (CTA pair, 256 x 256 tiles, 3 fp16 products per launch)",
             "ms_per_launch": {"forward": gf_ms / max(1, gf_n), "adjoint": ga_ms / max(1, ga_n)},
             "hbm_gbs_of_J_stream": j_bytes / (gemm_ms * 1e-3) / 1e9,
             "hbm_peak_gbs": peaks["hbm_gbs"]}

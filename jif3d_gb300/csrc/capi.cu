@@ -446,7 +446,9 @@ int build_stored(j3g_context *c, int storage) {
   const long long K = c->ngrid(), ldK = round64(K);
   const int NS = nstored(c);
   const long long R = (long long)c->nmeas * NS, ldR = round64(R);
-  const size_t need = storage == J3G_STORE_FP32 ? (size_t)R * ldK * 4 : (size_t)(R * ldK + K * ldR) * 4;
+  const size_t need = storage == J3G_STORE_FP32
+                          ? (size_t)R * ldK * 4
+                          : (size_t)(tiled_rows(R) * ldK + tiled_rows(K) * ldR) * 4;
   size_t fr = 0, tot = 0;
   J3G_CUDA(c, cudaMemGetInfo(&fr, &tot));
   if (need + (size_t)(1ull << 31) > fr)
@@ -473,10 +475,16 @@ int build_stored(j3g_context *c, int storage) {
       ++c->launches;
     }
   } else {
-    J3G_TRY(ensure(c, c->Jhi, 2 * (size_t)R * ldK));
-    J3G_TRY(ensure(c, c->Jlo, 2 * (size_t)R * ldK));
-    J3G_TRY(ensure(c, c->JThi, 2 * (size_t)K * ldR));
-    J3G_TRY(ensure(c, c->JTlo, 2 * (size_t)K * ldR));
+    // tiled layout; the padding rows of the last row block stay zero
+    const size_t bj = 2 * (size_t)tiled_rows(R) * ldK, bjt = 2 * (size_t)tiled_rows(K) * ldR;
+    J3G_TRY(ensure(c, c->Jhi, bj));
+    J3G_TRY(ensure(c, c->Jlo, bj));
+    J3G_TRY(ensure(c, c->JThi, bjt));
+    J3G_TRY(ensure(c, c->JTlo, bjt));
+    J3G_CUDA(c, cudaMemsetAsync(c->Jhi.p, 0, bj, c->stream));
+    J3G_CUDA(c, cudaMemsetAsync(c->Jlo.p, 0, bj, c->stream));
+    J3G_CUDA(c, cudaMemsetAsync(c->JThi.p, 0, bjt, c->stream));
+    J3G_CUDA(c, cudaMemsetAsync(c->JTlo.p, 0, bjt, c->stream));
     J3G_TRY(ensure(c, c->rowscale, sizeof(float) * (size_t)R));
     J3G_TRY(ensure(c, c->Jrowsum, sizeof(double) * (size_t)R));
     J3G_TRY(ensure(c, c->rows, sizeof(double) * (size_t)chunk * NS * K));
@@ -983,7 +991,8 @@ int j3g_sensitivity_info(const j3g_context *c, int *storage, long long *rows, lo
   if (cols) *cols = c->storage ? c->ngrid() : 0;
   if (bytes)
     *bytes = c->storage == J3G_STORE_FP32     ? c->st_rows * c->st_ld * 4
-             : c->storage == J3G_STORE_F16X2 ? 2 * (c->st_rows * c->st_ld * 2) + 2 * (c->ngrid() * c->st_ldT * 2)
+             : c->storage == J3G_STORE_F16X2 ? 2 * (tiled_rows(c->st_rows) * c->st_ld * 2) +
+                                                   2 * (tiled_rows(c->ngrid()) * c->st_ldT * 2)
                                               : 0;
   return J3G_OK;
 }

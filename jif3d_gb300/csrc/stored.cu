@@ -109,17 +109,17 @@ __global__ void k_split_rows(const double *__restrict__ rows, long long ld_in, l
     if (threadIdx.x == 0) rowsum[row0 + r] = acc;
   }
   const double inv = 1.0 / sc;
-  __half *h = hi + (row0 + r) * ld_out;
-  __half *l = lo + (row0 + r) * ld_out;
   for (long long c = threadIdx.x; c < ld_out; c += kT) {
     __half hv, lv;
     split_half(c < ncol ? p[c] * inv : 0.0, hv, lv);
-    h[c] = hv;
-    l[c] = lv;
+    const long long o = tiled_index(row0 + r, c, ld_out);
+    hi[o] = hv;
+    lo[o] = lv;
   }
 }
 
-// 32x32 tiled transpose of a 16-bit matrix [rows][ld_in] -> [cols][ld_out].
+// 32x32 blocked transpose of a 16-bit matrix, (r, c) -> (c, r), both in the
+// tiled layout (a 32-wide block never straddles a 64-column tile).
 __global__ void k_transpose16(const uint16_t *__restrict__ in, long long ld_in, long long rows,
                               long long cols, uint16_t *__restrict__ out, long long ld_out) {
   __shared__ uint16_t tile[32][34];
@@ -127,12 +127,12 @@ __global__ void k_transpose16(const uint16_t *__restrict__ in, long long ld_in, 
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
   for (int k = ty; k < 32; k += 8) {
     const long long r = r0 + k, c = c0 + tx;
-    tile[k][tx] = (r < rows && c < cols) ? in[r * ld_in + c] : (uint16_t)0;
+    tile[k][tx] = (r < rows && c < cols) ? in[tiled_index(r, c, ld_in)] : (uint16_t)0;
   }
   __syncthreads();
   for (int k = ty; k < 32; k += 8) {
     const long long c = c0 + k, r = r0 + tx;
-    if (c < cols && r < ld_out) out[c * ld_out + r] = tile[tx][k];
+    if (c < cols && r < ld_out) out[tiled_index(c, r, ld_out)] = tile[tx][k];
   }
 }
 

@@ -6,13 +6,28 @@
 
 namespace j3g {
 
+// Tiled layout of the stored fp16 sensitivity (the A operand of the
+// tensor-core products): tiles of 128 rows x 64 columns, each 16 KB
+// contiguous and row-major inside, ordered by column block within a row
+// block.  A matrix with rows padded to ld columns (a multiple of 64) and to a
+// multiple of 128 rows (tiled_rows) keeps element (r, c) at tiled_index.  One
+// TMA box of the products is one tile: a single contiguous 16 KB read,
+// where the row-major layout needed 128 separate 128-byte pieces.
+__host__ __device__ inline long long tiled_index(long long r, long long c, long long ld) {
+  return ((r >> 7) * (ld >> 6) + (c >> 6)) * 8192 + (r & 127) * 64 + (c & 63);
+}
+inline long long tiled_rows(long long rows) { return (rows + 127) / 128 * 128; }
+
 // fp16 hi / lo split of FP64 rows with a power-of-two row scale
-// (scale[row0 + r]): row = scale * (hi + lo), max|hi| in (2^13, 2^14].
+// (scale[row0 + r]): row = scale * (hi + lo), max|hi| in (2^13, 2^14];
+// hi / lo in the tiled layout with ld_out columns (padding columns zero).
 // rowsum (optional) receives the FP64 row sums J 1.
 cudaError_t launch_split_rows(const double *rows, long long ld_in, long long ncol, int nrows,
                               void *hi, void *lo, long long ld_out, float *scale, double *rowsum,
                               long long row0, cudaStream_t st);
-// out[c][r] = in[r][c] for r < rows (zero for rows <= r < ld_out), c < cols; 16-bit elements.
+// out(c, r) = in(r, c) for r < rows (zero for rows <= r < ld_out), c < cols;
+// 16-bit elements, both matrices in the tiled layout (in: ld_in columns,
+// out: ld_out columns).
 cudaError_t launch_transpose16(const void *in, long long ld_in, long long rows, long long cols,
                                void *out, long long ld_out, cudaStream_t st);
 // FP64 [nrow][ld_src] (column c times colscale[c] when given) -> fp16 hi / lo
@@ -57,8 +72,9 @@ cudaError_t launch_bg_grad_batched(int raw, int nmeas, int nbg, int nmod, const 
                                    const double *bgsens, double *grads, long long ld_grads,
                                    long long ngrid, cudaStream_t st);
 
-// Tensor-core products.  A [m][ld], B [n_pad][ld], K-major fp16 (or bf16), ld
-// a multiple of 64, n_pad a multiple of gemm_n_tile(n), 16-byte aligned bases.
+// Tensor-core products.  A: m rows x ld columns in the tiled layout (buffers of
+// tiled_rows(m) rows); B: [n_pad][ld] row-major; both K-major fp16 (or bf16),
+// ld a multiple of 64, n_pad a multiple of gemm_n_tile(n), 16-byte aligned bases.
 struct GemmOperands {
   const void *a_hi, *a_lo;  // 16-bit elements: bf16, or fp16 when f16 is set
   long long m;
