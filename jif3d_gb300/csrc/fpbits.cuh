@@ -64,9 +64,10 @@ __device__ __forceinline__ double f32_to_f64(float f) {
 }
 
 // d * 2^k for a normal d whose result stays normal, by an exponent add;
-// other cases (zero, subnormal, out of range) multiply.
+// zeros pass through; other cases (subnormal, out of range) multiply.
 __device__ __forceinline__ double scale_pow2(double d, int k) {
   const long long b = __double_as_longlong(d);
+  if ((b & 0x7fffffffffffffffLL) == 0) return d;
   const int e = (int)((b >> 52) & 0x7ff);
   if (e > 0 && e < 0x7ff && e + k > 0 && e + k < 0x7ff)
     return __longlong_as_double(b + ((long long)k << 52));

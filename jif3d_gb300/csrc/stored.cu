@@ -3,14 +3,15 @@
 // path, GravMag/FullSensitivityGravMagCalculator.h:136-221: d = J m and
 // g = 2 J^T r without recomputing any box term).
 //
-// Storage: row-major J (rows = station x stored component, columns = cells,
-// padded to a multiple of 64 columns with zeros), as
-//   FP32                       4 B per element, or
+// Storage: J with rows = station x stored component and columns = cells,
+// padded to a multiple of 64 columns with zeros, as
+//   FP32                       4 B per element, row-major, or
 //   FP16 hi + lo, row scale    2 x 2 B per element: J[r][c] ~= s_r (hi + lo),
 //                              s_r a power of two with max|J/s_r| in (2^13, 2^14],
 //                              hi = fp16(J/s_r), lo = fp16(J/s_r - hi) (22
-//                              significant bits), plus the transposed copy
-//                              used as the K-major operand of the adjoint GEMM.
+//                              significant bits), in 128 x 64 tiles (stored.h,
+//                              tiled_index), plus the transposed copy used as
+//                              the K-major operand of the adjoint GEMM.
 // Streaming products accumulate in FP32 in short chains and in FP64 across
 // chains; the tensor-core products are in gemm_tc.cu.
 #include <cuda_fp16.h>
@@ -349,54 +350,89 @@ __global__ void k_splitk_reduce(const float *__restrict__ P, int nsplit, long lo
   out[(long long)n * ld_out + r] = factor * v;
 }
 
-// The same over four consecutive rows per thread (nrow, ldp and slice multiples
-// of 4, P 16-byte aligned): float4 loads with kBatch splits in flight, and
-// the split sums accumulated as unevaluated FP32 pairs (hi + lo, error-free
-// two-sum), which carry about 48 bits -- as good as an FP64 sum of FP32
-// partials -- without the FP64 pipe.  Per output one FP64 add widens the pair;
-// the power-of-two scales are exponent adds.  factor is applied the same way
-// when it is a power of two (fpow2, 2^kfac), else by an FP64 multiply.
-__global__ void k_splitk_reduce4(const float *__restrict__ P, int nsplit, long long slice,
-                                 int nmod, int nrow, long long ldp,
-                                 const float *__restrict__ rowscale,
-                                 const float *__restrict__ modscale,
-                                 const double *__restrict__ modmean,
-                                 const double *__restrict__ rowsum, bool fpow2, int kfac,
-                                 double factor, double *__restrict__ out, long long ld_out) {
+// The same over groups of four consecutive rows (nrow, ldp and slice
+// multiples of 4, P 16-byte aligned); grid (row blocks, models), no index
+// division.  A thread takes kGroups groups kT quads apart within one model --
+// consecutive threads read consecutive float4s -- and two splits at a time, so
+// that eight independent 16-byte loads are in flight per thread whatever the
+// number of splits.  The split sums accumulate as unevaluated FP32 pairs
+// (hi + lo, error-free two-sum), about 48 bits -- as good as an FP64 sum of
+// FP32 partials -- without the FP64 pipe.  With more than kPairSplits splits
+// one FP64 add per output widens the pair; with fewer the pair is rounded to
+// FP32 first (relative 2^-24, below the FP32 rounding each partial already
+// carries) so that the pass stays at HBM speed: one FP64 operation per output
+// costs as much as the whole memory traffic on this GPU's FP64 pipe.  The
+// power-of-two scales are exponent adds; factor is applied the same way when
+// it is a power of two (fpow2, 2^kfac), else by an FP64 multiply.
+constexpr int kGroups = 4;
+constexpr int kPairSplits = 4;
+template <bool PAIR>  // PAIR: widen hi + lo in FP64 (more than kPairSplits splits)
+__global__ void __launch_bounds__(kT) k_splitk_reduce4(
+    const float *__restrict__ P, int nsplit, long long slice, int nrow, long long ldp,
+    const float *__restrict__ rowscale, const float *__restrict__ modscale,
+    const double *__restrict__ modmean, const double *__restrict__ rowsum, bool fpow2, int kfac,
+    double factor, double *__restrict__ out, long long ld_out) {
   const int nq = nrow / 4;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)nmod * nq) return;
-  const int n = (int)(t / nq), r = (int)(t % nq) * 4;
-  const float4 *p = reinterpret_cast<const float4 *>(P + (long long)n * ldp + r);
+  const int n = blockIdx.y;
+  const int q0 = blockIdx.x * (kT * kGroups) + threadIdx.x;
   const long long s4 = slice / 4;
-  float hi[4] = {0.0f, 0.0f, 0.0f, 0.0f}, lo[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-  auto add4 = [&](const float4 &q) {
-    const float x[4] = {q.x, q.y, q.z, q.w};
+  const float4 *p = reinterpret_cast<const float4 *>(P + (long long)n * ldp);
+  float hi[kGroups][4], lo[kGroups][4];
+#pragma unroll
+  for (int g = 0; g < kGroups; ++g)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) hi[g][i] = lo[g][i] = 0.0f;
+  for (int s = 0; s < nsplit; s += 2) {
+    float4 q[kGroups][2];
+#pragma unroll
+    for (int g = 0; g < kGroups; ++g)
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        const int qi = q0 + g * kT;
+        q[g][u] = (qi < nq && s + u < nsplit) ? __ldcs(p + (long long)(s + u) * s4 + qi)
+                                              : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+    for (int g = 0; g < kGroups; ++g)
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        if (s + u >= nsplit) continue;
+        const float x[4] = {q[g][u].x, q[g][u].y, q[g][u].z, q[g][u].w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          float sres, err;
+          two_sum(hi[g][i], x[i], sres, err);
+          hi[g][i] = sres;
+          lo[g][i] = __fadd_rn(lo[g][i], err);
+        }
+      }
+  }
+  const int kmod = (modscale ? pow2_exponent(modscale[n]) : 0) + (fpow2 ? kfac : 0);
+#pragma unroll
+  for (int g = 0; g < kGroups; ++g) {
+    const int qi = q0 + g * kT;
+    if (qi >= nq) continue;
+    const int r = qi * 4;
+    double res[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      float sres, err;
-      two_sum(hi[i], x[i], sres, err);
-      hi[i] = sres;
-      lo[i] = __fadd_rn(lo[i], err);
+      // a compile-time choice: as a run-time select both arms were evaluated
+      double v = PAIR ? f32_to_f64(hi[g][i]) + f32_to_f64(lo[g][i])
+                      : f32_to_f64(__fadd_rn(hi[g][i], lo[g][i]));
+      v = scale_pow2(v, kmod + (rowscale ? pow2_exponent(rowscale[r + i]) : 0));
+      if (modmean)
+        v = fma(modmean[n], fpow2 ? scale_pow2(rowsum[r + i], kfac) : rowsum[r + i], v);
+      res[i] = fpow2 ? v : factor * v;
     }
-  };
-  int s = 0;
-  for (; s + kBatch <= nsplit; s += kBatch) {
-    float4 q[kBatch];
+    double *o = out + (long long)n * ld_out + r;
+    // whole 16-byte stores where the output row allows (full sectors per warp)
+    if ((reinterpret_cast<uintptr_t>(o) & 15) == 0) {
+      __stcs(reinterpret_cast<double2 *>(o), make_double2(res[0], res[1]));
+      __stcs(reinterpret_cast<double2 *>(o) + 1, make_double2(res[2], res[3]));
+    } else {
 #pragma unroll
-    for (int u = 0; u < kBatch; ++u) q[u] = __ldcs(p + (long long)(s + u) * s4);
-#pragma unroll
-    for (int u = 0; u < kBatch; ++u) add4(q[u]);
-  }
-  for (; s < nsplit; ++s) add4(__ldcs(p + (long long)s * s4));
-  const int kmod = (modscale ? pow2_exponent(modscale[n]) : 0) + (fpow2 ? kfac : 0);
-  double *o = out + (long long)n * ld_out + r;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    double v = f32_to_f64(hi[i]) + f32_to_f64(lo[i]);
-    v = scale_pow2(v, kmod + (rowscale ? pow2_exponent(rowscale[r + i]) : 0));
-    if (modmean) v = fma(modmean[n], fpow2 ? scale_pow2(rowsum[r + i], kfac) : rowsum[r + i], v);
-    o[i] = fpow2 ? v : factor * v;
+      for (int i = 0; i < 4; ++i) o[i] = res[i];
+    }
   }
 }
 
@@ -586,13 +622,19 @@ cudaError_t launch_splitk_reduce(const float *P, int nsplit, long long slice, in
                                  double *out, long long ld_out, cudaStream_t st) {
   const long long n = (long long)nmod * nrow;
   if (n == 0) return cudaSuccess;
-  if (nrow % 4 == 0 && ldp % 4 == 0 && slice % 4 == 0 &&
+  if (nrow % 4 == 0 && ldp % 4 == 0 && slice % 4 == 0 && nmod <= 65535 &&
       (reinterpret_cast<uintptr_t>(P) & 15) == 0) {
     int kf = 0;
     const bool fpow2 = factor != 0.0 && std::frexp(factor, &kf) == 0.5;  // factor = 2^(kf-1)
-    k_splitk_reduce4<<<cdiv(n / 4, kT), kT, 0, st>>>(P, nsplit, slice, nmod, nrow, ldp, rowscale,
-                                                      modscale, modmean, rowsum, fpow2, kf - 1,
-                                                      factor, out, ld_out);
+    dim3 grid(cdiv(nrow / 4, (long long)kT * kGroups), nmod);
+    if (nsplit > kPairSplits)
+      k_splitk_reduce4<true><<<grid, kT, 0, st>>>(P, nsplit, slice, nrow, ldp, rowscale, modscale,
+                                                  modmean, rowsum, fpow2, kf - 1, factor, out,
+                                                  ld_out);
+    else
+      k_splitk_reduce4<false><<<grid, kT, 0, st>>>(P, nsplit, slice, nrow, ldp, rowscale,
+                                                   modscale, modmean, rowsum, fpow2, kf - 1,
+                                                   factor, out, ld_out);
     return cudaGetLastError();
   }
   k_splitk_reduce<<<cdiv(n, kT), kT, 0, st>>>(P, nsplit, slice, nmod, nrow, ldp, rowscale,

@@ -4,9 +4,11 @@
     python -m jif3d_gb300.profiling fp64-weights           # libm FP64 weight probes
     python -m jif3d_gb300.profiling gemm [--stations 128]  # tensor-core batched products
     python -m jif3d_gb300.profiling stream [--stations 400] # FP32 streaming products
+    python -m jif3d_gb300.profiling batched [--steps 2]     # full config-4 batched steps
 
 Each case runs a few launches on a few-MB problem so that an ncu capture of
-it ends by itself.
+it ends by itself; ``batched`` runs the full 256-model config-4 step (7.5 GB of
+stored J) for a launch list with one-pass metrics only.
 """
 from __future__ import annotations
 
@@ -67,6 +69,31 @@ def case_stream(stations: int) -> None:
     ctx.close()
 
 
+def case_batched(steps: int) -> None:
+    """The batched benchmark step on config 4 (256 models): batched forward,
+    weighted misfit, batched adjoint, after the sensitivity build."""
+    import torch
+    from . import capi, workloads as W
+    s = W.config4()
+    ctx = capi.Context(0)
+    W.setup_context(ctx, s)
+    n = s.stations.shape[0]
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    models = torch.tensor(s.models, dtype=torch.float64, device="cuda")
+    nmod = models.shape[0]
+    data = torch.zeros((nmod, n * 10), dtype=torch.float64, device="cuda")
+    obs = torch.zeros(n * 10, dtype=torch.float64, device="cuda")
+    grads = torch.zeros_like(models)
+    for _ in range(steps):
+        ctx.batched_forward_device(nmod, models.data_ptr(), data.data_ptr())
+        misfit = (data - obs).contiguous()
+        ctx.batched_lqderivative_device(nmod, models.data_ptr(), misfit.data_ptr(),
+                                        grads.data_ptr())
+    ctx.synchronize()
+    print("batched case ok", n, "stations", nmod, "models", float(grads[0, 0]))
+    ctx.close()
+
+
 def case_fp64_weights(n_iter: int) -> None:
     from . import capi
     lib = capi.load()
@@ -88,6 +115,8 @@ def main(argv=None) -> None:
     g.add_argument("--models", type=int, default=256)
     st = sub.add_parser("stream")
     st.add_argument("--stations", type=int, default=400)
+    b = sub.add_parser("batched")
+    b.add_argument("--steps", type=int, default=2)
     a = p.parse_args(argv)
     if a.case == "node":
         case_node(a.stations)
@@ -95,6 +124,8 @@ def main(argv=None) -> None:
         case_gemm(a.stations, a.models)
     elif a.case == "stream":
         case_stream(a.stations)
+    elif a.case == "batched":
+        case_batched(a.steps)
     elif a.case == "fp64-weights":
         case_fp64_weights(a.iters)
 

@@ -79,6 +79,8 @@ __global__ void k_misc(unsigned long long n, unsigned long long *bad) {
     nb[0] += !(ev == ea && (a < 0) == (v < 0) && fabs((double)a - v) < ldexp(fabs(v), -20));
     const int k = (int)(mix64(r + 1) % 121) - 60;
     nb[1] += __double_as_longlong(scale_pow2(v, k)) != __double_as_longlong(v * ldexp(1.0, k));
+    const double z = (r & 2) ? -0.0 : 0.0;  // zeros keep their sign
+    nb[1] += __double_as_longlong(scale_pow2(z, k)) != __double_as_longlong(z);
     const float x = __uint_as_float((uint32_t)r & 0xbfffffffu);  // finite, |x| < 2
     const float y = __uint_as_float((uint32_t)(r >> 32) & 0xbfffffffu);
     float s, err;
