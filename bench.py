@@ -130,6 +130,13 @@ def max_over_ranks(v, world):
     return float(t.item())
 
 
+# DRAM traffic of one tensor-core product launch on config 4 with 256 models,
+# measured with ncu (one-pass dram__bytes_read.sum + dram__bytes_write.sum on
+# the full-size launches of `python -m jif3d_gb300.profiling batched`):
+# forward 3934.5 + 219.2 MB, adjoint 3813.1 + 257.6 MB.
+GEMM_DRAM_BYTES_PER_LAUNCH = 0.5 * ((3934.5 + 219.2) + (3813.1 + 257.6)) * 1e6
+
+
 def sigma_vector(s):
     n = s.stations.shape[0]
     return np.tile(np.array([SIGMA_GZ] + [SIGMA_U] * 9), n)
@@ -278,7 +285,13 @@ def run_batched(args, rank, world, local):
     # fp16 and bf16 MMA (kind::f16) share one dense rate; the measured cuBLAS
     # bf16 figure is the denominator
     roof = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"],
-            "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"], "traffic": None,
+            "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"],
+            "traffic": GEMM_DRAM_BYTES_PER_LAUNCH, "traffic_unit": "DRAM bytes per launch",
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
+                              "full-size config-4 launches (mean of forward and adjoint)",
+            # J hi + lo and the forward's model hi + lo, read once; the
+            # per-split partial sums (235-268 MB) come on top
+            "algorithmic_bytes_per_launch": j_bytes + 4 * nmod * K,
             "peak_source": f"{src} bf16_tflops (burst; fp16 MMA runs at the bf16 rate)",
             "kernel": "k_gemm_pair<fp16> (CTA pair, 256 x 256 tiles, 3 fp16 products per launch)",
             "ms_per_launch": {"forward": gf_ms / max(1, gf_n), "adjoint": ga_ms / max(1, ga_n)},
