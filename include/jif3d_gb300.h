@@ -11,9 +11,11 @@
  *   model cell (xi, yi, zi) at offset (xi*ny + yi)*nz + zi, z fastest, z down
  *     (ModelBase/ThreeDModelBase.h:157-168);
  *   model vectors hold ngrid grid values followed by nbg background values
- *     (Gravity/ThreeDGravityModel.h:91-99);
+ *     (Gravity/ThreeDGravityModel.h:91-99), magnetisation models three ngrid
+ *     blocks (x, y, z) and no background;
  *   raw data per station: scalar 1 (g_z), tensor 9 (Uxx..Uzz, C order),
- *     magnetic 3 (Bx, By, Bz), joint 10 (g_z then the 9 tensor values);
+ *     magnetic 3 (Bx, By, Bz), joint 10 (g_z then the 9 tensor values),
+ *     vertical magnetic gradient 1, magnetisation 3 (Bx, By, Bz);
  *   sensitivity rows are row-major, nmeas*raw rows of ngrid+nbg columns
  *     (GravMag/FullSensitivityGravMagCalculator.h:116-130);
  *   angles in radians, field strength in nT, densities in kg/m^3, SI output.
@@ -44,7 +46,18 @@ enum j3g_kind {
   J3G_SCALAR = 1,   /* g_z,             ScalarOMPGravityImp / ScalarCudaGravityImp */
   J3G_TENSOR = 2,   /* FTG 9 components, TensorOMPGravityImp / TensorCudaGravityImp */
   J3G_MAGNETIC = 3, /* induced B,        OMPMagneticSusceptibilityImp / CudaMagneticSusceptibilityImp */
-  J3G_JOINT = 4     /* g_z + FTG in one pass (no single reference counterpart) */
+  J3G_JOINT = 4,    /* g_z + FTG in one pass (no single reference counterpart) */
+  /* vertical gradient of Bz, one datum per station: Bz(z) - Bz(z + 1 m),
+   * Magnetics/OMPMagneticGradImp.cpp:13-106.  Model ngrid susceptibilities +
+   * nbg background values, the background does not respond (its gradient is
+   * zero, OMPMagneticGradImp.h:32-40).  Transform: none. */
+  J3G_MAG_GRADIENT = 5,
+  /* remanent magnetisation, Bx By Bz per station,
+   * Magnetics/OMPMagnetizationImp.cpp:25-117.  Model 3 * ngrid values: the x,
+   * y and z magnetisation blocks (ThreeDMagnetizationModel.h:53-70), no
+   * background.  Transforms: none, total field, total-field anomaly.  Not
+   * available for the device-resident sensitivity (j3g_build_sensitivity). */
+  J3G_MAGNETIZATION = 6
 };
 
 enum j3g_transform {

@@ -14,7 +14,7 @@ import numpy as np
 from . import build as _build
 
 OK, ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_UNSUPPORTED, ERR_SCRATCH_LIMIT = range(7)
-SCALAR, TENSOR, MAGNETIC, JOINT = 1, 2, 3, 4
+SCALAR, TENSOR, MAGNETIC, JOINT, MAG_GRADIENT, MAGNETIZATION = 1, 2, 3, 4, 5, 6
 T_NONE, T_FTG_INVARIANT, T_TOTAL_FIELD, T_TFA = 0, 1, 2, 3
 STORE_FP32, STORE_F16X2 = 1, 2
 (TIMER_NODE_FORWARD, TIMER_NODE_ADJOINT, TIMER_STREAM_FORWARD, TIMER_STREAM_ADJOINT,

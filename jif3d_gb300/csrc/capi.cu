@@ -73,7 +73,15 @@ struct j3g_context {
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> timed;
 
   long long ngrid() const { return (long long)nx * ny * nz; }
-  long long nparm() const { return ngrid() + (long long)bg.size(); }
+  // model blocks: magnetisation has three cell blocks and no background
+  // parameters (Magnetics/ThreeDMagnetizationModel.h:66-69)
+  long long nparm() const {
+    return kind == J3G_MAGNETIZATION ? 3 * ngrid() : ngrid() + (long long)bg.size();
+  }
+  long long ngrid_cols() const { return (long long)kind_nblock(kind) * ngrid(); }
+  // background layers that respond (none for the vertical gradient and
+  // magnetisation: OMPMagneticGradImp.h:32-40, OMPMagnetizationImp.cpp:16-22)
+  int nbg_active() const { return kind_special(kind) ? 0 : (int)bg.size(); }
   long long nnodes() const { return (long long)(nx + 1) * (ny + 1) * (nz + 1); }
   int raw() const { return kind_raw(kind); }
   int dpm() const { return transform == J3G_T_NONE ? raw() : 1; }
@@ -191,7 +199,15 @@ MagField mag_field(const j3g_context *c) {
   m.by = std::cos(c->inc) * std::sin(c->dec);
   m.bz = std::sin(c->inc);
   m.fs = c->fs;
-  m.factor = 1.0 / (4 * 3.141592653589793238462643383279502884 * kGravConst);
+  const double pi = 3.141592653589793238462643383279502884;
+  if (c->kind == J3G_MAG_GRADIENT) {
+    m.factor = 1e-7 / kGravConst;  // Magnetics/OMPMagneticGradImp.cpp:66
+  } else if (c->kind == J3G_MAGNETIZATION) {
+    const double mag_mu = 4e-7 * pi;  // Magnetics/OMPMagnetizationImp.cpp:29, 58-59
+    m.factor = 1.0e9 * mag_mu / (4 * pi * kGravConst);
+  } else {
+    m.factor = 1.0 / (4 * pi * kGravConst);
+  }
   return m;
 }
 
@@ -214,7 +230,7 @@ int check_ready(j3g_context *c) {
 
 // Background sensitivities of every station (cached until geometry changes).
 int ensure_background(j3g_context *c) {
-  const int nbg = (int)c->bg.size();
+  const int nbg = c->nbg_active();
   if (nbg == 0) return J3G_OK;
   if (!c->bg_dirty) return J3G_OK;
   J3G_TRY(ensure(c, c->bgsens, sizeof(double) * (size_t)c->nmeas * c->raw() * nbg));
@@ -234,9 +250,12 @@ constexpr int kTargetBlocks = 152 * 8;
 // Gridded node-component sums comps[nmeas][NC_COUNT] for the model d_model.
 int gridded_node_forward(j3g_context *c, const double *d_model) {
   const long long nn = c->nnodes();
-  J3G_TRY(ensure(c, c->rhot, sizeof(double) * nn));
+  const int nblock = kind_nblock(c->kind);
+  J3G_TRY(ensure(c, c->rhot, sizeof(double) * nn * nblock));
   MeshView m = mesh_view(c);
-  J3G_LAUNCH(c, launch_rho_tilde(m, d_model, ptr<double>(c->rhot), c->stream));
+  for (int b = 0; b < nblock; ++b)
+    J3G_LAUNCH(c, launch_rho_tilde(m, d_model + (size_t)b * c->ngrid(),
+                                   ptr<double>(c->rhot) + (size_t)b * nn, c->stream));
   int npb = 2048, spb = 4;
   auto blocks = [&](int a, int b) {
     return ((nn + a - 1) / a) * (long long)((c->nmeas + b - 1) / b);
@@ -253,7 +272,7 @@ int gridded_node_forward(j3g_context *c, const double *d_model) {
                                       ptr<double>(c->partial), nblk, npb, spb, c->stream));
   }
   J3G_LAUNCH(c, launch_forward_reduce(c->kind, c->nmeas, nblk, ptr<double>(c->partial),
-                                    ptr<double>(c->comps), c->stream));
+                                      mag_field(c), ptr<double>(c->comps), c->stream));
   return J3G_OK;
 }
 
@@ -271,9 +290,11 @@ int row_chunk(j3g_context *c, long long ld) {
 // Raw gridded data from explicit sensitivity rows: rowsum[nmeas][raw].
 // Optionally copies each chunk's rows (with background columns) to h_sens.
 int gridded_rows_forward(j3g_context *c, const double *d_model, double *h_sens) {
-  const long long ngrid = c->ngrid(), nparm = c->nparm();
-  const int raw = c->raw(), nbg = (int)c->bg.size();
-  const long long ld = h_sens ? nparm : ngrid;
+  const long long ngrid = c->ngrid(), nparm = c->nparm(), ncolg = c->ngrid_cols();
+  const int raw = c->raw(), nbg = c->nbg_active();
+  // background columns without a response (vertical gradient) are zero
+  const int nbg_zero = c->kind == J3G_MAG_GRADIENT ? (int)c->bg.size() : 0;
+  const long long ld = h_sens ? nparm : ncolg;
   const int chunk = row_chunk(c, ld);
   J3G_TRY(ensure(c, c->rows, sizeof(double) * (size_t)chunk * raw * ld));
   if (c->node_exact)
@@ -288,13 +309,16 @@ int gridded_rows_forward(j3g_context *c, const double *d_model, double *h_sens) 
       J3G_LAUNCH(c, launch_sens_rows(c->kind, c->node_exact, m, s, s0, ns, mf, ptr<double>(c->F),
                                    ptr<double>(c->rows), ld, c->stream));
       if (c->node_exact) ++c->launches;  // node terms + cell combine
-      J3G_LAUNCH(c, launch_rows_dot(raw, ns, ngrid, ptr<double>(c->rows), ld, d_model,
+      J3G_LAUNCH(c, launch_rows_dot(raw, ns, ncolg, ptr<double>(c->rows), ld, d_model,
                                   ptr<double>(c->rowsum) + (size_t)s0 * raw, c->stream));
     } else {
       J3G_CUDA(c, cudaMemsetAsync(ptr<double>(c->rowsum) + (size_t)s0 * raw, 0,
                                   sizeof(double) * ns * raw, c->stream));
     }
     if (h_sens) {
+      if (nbg_zero > 0)
+        J3G_CUDA(c, cudaMemset2DAsync(ptr<double>(c->rows) + ngrid, ld * sizeof(double), 0,
+                                      nbg_zero * sizeof(double), (size_t)ns * raw, c->stream));
       if (nbg > 0)
         J3G_CUDA(c, cudaMemcpy2DAsync(ptr<double>(c->rows) + ngrid, ld * sizeof(double),
                                       ptr<double>(c->bgsens) + (size_t)s0 * raw * nbg,
@@ -317,9 +341,11 @@ int forward_device(j3g_context *c, const double *d_model, double *d_data, double
   J3G_TRY(ensure_background(c));
   double tbx, tby, tbz;
   tfa_dir(c, tbx, tby, tbz);
-  const int nbg = (int)c->bg.size();
+  const int nbg = c->nbg_active();
   const double *bgval = d_model + c->ngrid();
   const double *bgsens = nbg ? ptr<double>(c->bgsens) : nullptr;
+  // node sums per station: node components, or raw rows for the special kinds
+  const int comps_ld = kind_special(c->kind) ? c->raw() : NC_COUNT;
   if (h_sens || (!c->node_exact && c->ngrid() > 0)) {
     J3G_TRY(gridded_rows_forward(c, d_model, h_sens));
     J3G_LAUNCH(c, launch_assemble(c->kind, c->transform, tbx, tby, tbz, c->nmeas,
@@ -333,7 +359,7 @@ int forward_device(j3g_context *c, const double *d_model, double *d_data, double
       J3G_CUDA(c, cudaMemsetAsync(c->comps.p, 0, sizeof(double) * c->nmeas * NC_COUNT, c->stream));
     }
     J3G_LAUNCH(c, launch_assemble(c->kind, c->transform, tbx, tby, tbz, c->nmeas,
-                                ptr<double>(c->comps), NC_COUNT, bgsens, nbg, bgval, mag_field(c),
+                                ptr<double>(c->comps), comps_ld, bgsens, nbg, bgval, mag_field(c),
                                 raw_out, d_data, c->stream));
   }
   return J3G_OK;
@@ -348,7 +374,9 @@ int adjoint_device(j3g_context *c, const double *d_model, const double *d_misfit
     return J3G_OK;
   }
   J3G_TRY(ensure_background(c));
-  const int raw = c->raw(), nbg = (int)c->bg.size();
+  const int raw = c->raw(), nbg = c->nbg_active();
+  const long long ncolg = c->ngrid_cols();
+  const int nblock = kind_nblock(c->kind);
   double tbx, tby, tbz;
   tfa_dir(c, tbx, tby, tbz);
   const double *rawd = nullptr;
@@ -365,7 +393,7 @@ int adjoint_device(j3g_context *c, const double *d_model, const double *d_misfit
   MeshView m = mesh_view(c);
   StationView s = station_view(c);
   if (ngrid > 0 && c->node_exact) {
-    J3G_TRY(ensure(c, c->W, sizeof(double) * (size_t)c->nmeas * NC_COUNT));
+    J3G_TRY(ensure(c, c->W, sizeof(double) * (size_t)c->nmeas * std::max<int>(NC_COUNT, kMaxVc)));
     J3G_LAUNCH(c, launch_comp_weights(c->kind, c->nmeas, ptr<double>(c->wraw), mag_field(c),
                                     ptr<double>(c->W), c->stream));
     const long long nn = c->nnodes();
@@ -375,38 +403,40 @@ int adjoint_device(j3g_context *c, const double *d_model, const double *d_misfit
     int nchunk = (int)std::max(1LL, std::min(want, maxchunk));
     const int spc = (c->nmeas + nchunk - 1) / nchunk;
     nchunk = (c->nmeas + spc - 1) / spc;
-    J3G_TRY(ensure(c, c->Gpart, sizeof(double) * (size_t)nchunk * nn));
-    J3G_TRY(ensure(c, c->G, sizeof(double) * (size_t)nn));
+    J3G_TRY(ensure(c, c->Gpart, sizeof(double) * (size_t)nchunk * nblock * nn));
+    J3G_TRY(ensure(c, c->G, sizeof(double) * (size_t)nblock * nn));
     {
       TimedScope ts(c, J3G_TIMER_NODE_ADJOINT);
       J3G_LAUNCH(c, launch_node_adjoint(c->kind, m, s, ptr<double>(c->W), spc, nchunk,
                                         ptr<double>(c->Gpart), c->stream));
     }
-    J3G_LAUNCH(c, launch_adjoint_combine(m, nchunk, ptr<double>(c->Gpart), ptr<double>(c->G),
-                                       d_grad, c->stream));
-    ++c->launches;  // chunk sum + cell combine
+    J3G_LAUNCH(c, launch_adjoint_combine(m, nchunk, nblock, ptr<double>(c->Gpart),
+                                         ptr<double>(c->G), d_grad, c->stream));
+    c->launches += 2 * nblock - 1;  // chunk sum + cell combine per block
   } else if (ngrid > 0) {
     // eight-corner rows, accumulated chunk by chunk
-    J3G_CUDA(c, cudaMemsetAsync(d_grad, 0, sizeof(double) * (size_t)ngrid, c->stream));
-    const int chunk = row_chunk(c, ngrid);
-    J3G_TRY(ensure(c, c->rows, sizeof(double) * (size_t)chunk * raw * ngrid));
+    J3G_CUDA(c, cudaMemsetAsync(d_grad, 0, sizeof(double) * (size_t)ncolg, c->stream));
+    const int chunk = row_chunk(c, ncolg);
+    J3G_TRY(ensure(c, c->rows, sizeof(double) * (size_t)chunk * raw * ncolg));
     const MagField mf = mag_field(c);
     for (int s0 = 0; s0 < c->nmeas; s0 += chunk) {
       const int ns = std::min(chunk, c->nmeas - s0);
       J3G_LAUNCH(c, launch_sens_rows(c->kind, false, m, s, s0, ns, mf, nullptr,
-                                   ptr<double>(c->rows), ngrid, c->stream));
-      J3G_LAUNCH(c, launch_rows_tdot(ns * raw, ngrid, ptr<double>(c->rows), ngrid,
+                                   ptr<double>(c->rows), ncolg, c->stream));
+      J3G_LAUNCH(c, launch_rows_tdot(ns * raw, ncolg, ptr<double>(c->rows), ncolg,
                                    ptr<double>(c->wraw) + (size_t)s0 * raw, d_grad, c->stream));
     }
-    J3G_LAUNCH(c, launch_scale(ngrid, 2.0, d_grad, c->stream));
+    J3G_LAUNCH(c, launch_scale(ncolg, 2.0, d_grad, c->stream));
   }
+  if (c->kind == J3G_MAG_GRADIENT && !c->bg.empty())  // background parameters do not respond
+    J3G_CUDA(c, cudaMemsetAsync(d_grad + ngrid, 0, sizeof(double) * c->bg.size(), c->stream));
   if (nbg > 0)
     J3G_LAUNCH(c, launch_background_grad(c->kind, c->nmeas, nbg, ptr<double>(c->wraw),
                                        ptr<double>(c->bgsens), d_grad + ngrid, c->stream));
   return J3G_OK;
 }
 
-bool valid_kind(int k) { return k >= J3G_SCALAR && k <= J3G_JOINT; }
+bool valid_kind(int k) { return k >= J3G_SCALAR && k <= J3G_MAGNETIZATION; }
 
 // ---------------------------------------------------------------------------
 // Device-resident sensitivity (the GPU side of FullSensitivityGravMagCalculator)
@@ -437,6 +467,9 @@ int build_stored(j3g_context *c, int storage) {
   J3G_TRY(check_ready(c));
   if (storage != J3G_STORE_FP32 && storage != J3G_STORE_F16X2)
     return fail(c, J3G_ERR_ARG, "unknown storage");
+  if (kind_special(c->kind))
+    return fail(c, J3G_ERR_UNSUPPORTED,
+                "device sensitivity is built for gravity, FTG and induced magnetics only");
   if (!c->node_exact)
     return fail(c, J3G_ERR_UNSUPPORTED,
                 "device sensitivity needs corner coordinates that are running sums of the sizes");
@@ -879,7 +912,7 @@ int j3g_set_kind(j3g_context *c, int kind, double inc, double dec, double fs) {
   if (c->transform != J3G_T_NONE) {
     const bool ok = (c->transform == J3G_T_FTG_INVARIANT && kind == J3G_TENSOR) ||
                     ((c->transform == J3G_T_TOTAL_FIELD || c->transform == J3G_T_TFA) &&
-                     kind == J3G_MAGNETIC);
+                     (kind == J3G_MAGNETIC || kind == J3G_MAGNETIZATION));
     if (!ok) c->transform = J3G_T_NONE;
   }
   return J3G_OK;
@@ -891,8 +924,9 @@ int j3g_set_transform(j3g_context *c, int transform, double inc, double dec) {
     return fail(c, J3G_ERR_ARG, "unknown transform");
   if (transform == J3G_T_FTG_INVARIANT && c->kind != J3G_TENSOR)
     return fail(c, J3G_ERR_UNSUPPORTED, "the FTG invariant needs tensor data");
-  if ((transform == J3G_T_TOTAL_FIELD || transform == J3G_T_TFA) && c->kind != J3G_MAGNETIC)
-    return fail(c, J3G_ERR_UNSUPPORTED, "total-field transforms need magnetic data");
+  if ((transform == J3G_T_TOTAL_FIELD || transform == J3G_T_TFA) && c->kind != J3G_MAGNETIC &&
+      c->kind != J3G_MAGNETIZATION)
+    return fail(c, J3G_ERR_UNSUPPORTED, "total-field transforms need three-component magnetic data");
   c->transform = transform;
   c->tinc = inc;
   c->tdec = dec;

@@ -132,7 +132,7 @@ extern "C" int j3g_forward_noalloc(int kind, int nx, int ny, int nz, const doubl
   if (launch_rho_tilde(m, d_model, rho_t, st) != cudaSuccess) return J3G_ERR_CUDA;
   if (launch_node_forward(kind, m, s, rho_t, partial, nblk, npb, spb, st) != cudaSuccess)
     return J3G_ERR_CUDA;
-  if (launch_forward_reduce(kind, nmeas, nblk, partial, comps, st) != cudaSuccess)
+  if (launch_forward_reduce(kind, nmeas, nblk, partial, mf, comps, st) != cudaSuccess)
     return J3G_ERR_CUDA;
   if (launch_assemble(kind, TR_NONE, 0.0, 0.0, 0.0, nmeas, comps, NC_COUNT, nullptr, 0, nullptr,
                       mf, nullptr, d_data, st) != cudaSuccess)

@@ -68,9 +68,9 @@ template <int KIND>
 __global__ void __launch_bounds__(kThreads)
     k_node_forward(MeshView m, StationView st, const double *__restrict__ rt,
                    double *__restrict__ partial, int npb, int spb) {
-  constexpr int MASK = KindTraits<KIND>::mask;
-  constexpr int NCMP = KindTraits<KIND>::ncomp;
-  constexpr int OFF = Slots<KIND>::off;
+  using T = KindTraits<KIND>;
+  constexpr int MASK = T::mask;
+  constexpr int NCMP = T::ncomp;
   const int ny1 = m.ny + 1, nz1 = m.nz + 1;
   const int nn = (m.nx + 1) * ny1 * nz1;
   const int n0 = blockIdx.x * npb;
@@ -81,17 +81,24 @@ __global__ void __launch_bounds__(kThreads)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int s = s0; s < s1; ++s) {
     const double mx = st.x[s], my = st.y[s], mz = st.z[s];
+    // the second position of the vertical gradient, z_meas + 1 as the
+    // reference forms it (OMPMagneticGradImp.cpp:76-79)
+    const double mz1 = T::twin ? add(mz, 1.0) : mz;
     double acc[NCMP];
 #pragma unroll
     for (int q = 0; q < NCMP; ++q) acc[q] = 0.0;
     for (int n = n0 + threadIdx.x; n < n1; n += kThreads) {
       int i, j, k;
       decode_node(n, ny1, nz1, i, j, k);
-      double F[NC_COUNT];
-      node_terms<MASK>(sub(mx, m.X[i]), sub(my, m.Y[j]), sub(mz, m.Z[k]), F);
-      const double w = rt[n];
+      double F[T::twin ? 2 : 1][NC_COUNT];
+      const double dx = sub(mx, m.X[i]), dy = sub(my, m.Y[j]);
+      node_terms<MASK>(dx, dy, sub(mz, m.Z[k]), F[0]);
+      if constexpr (T::twin) node_terms<MASK>(dx, dy, sub(mz1, m.Z[k]), F[T::twin ? 1 : 0]);
+      double w[T::nblock];
 #pragma unroll
-      for (int q = 0; q < NCMP; ++q) acc[q] = fma(F[q + OFF], w, acc[q]);
+      for (int b = 0; b < T::nblock; ++b) w[b] = rt[(long long)b * nn + n];
+#pragma unroll
+      for (int q = 0; q < NCMP; ++q) acc[q] = fma(F[T::at(q)][T::comp(q)], w[T::block(q)], acc[q]);
     }
 #pragma unroll
     for (int q = 0; q < NCMP; ++q) {
@@ -126,6 +133,26 @@ __global__ void k_forward_reduce(int nmeas, int nblk, const double *__restrict__
   comps[t] = v;
 }
 
+// The special kinds: virtual components straight to raw rows[nmeas][raw].
+template <int KIND>
+__global__ void k_forward_reduce_raw(int nmeas, int nblk, const double *__restrict__ partial,
+                                     MagField mf, double *__restrict__ rawrows) {
+  using T = KindTraits<KIND>;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nmeas) return;
+  double v[kMaxVc];
+#pragma unroll
+  for (int q = 0; q < T::ncomp; ++q) {
+    double a = 0.0;
+    for (int b = 0; b < nblk; ++b) a += partial[((long long)b * nmeas + s) * T::ncomp + q];
+    v[q] = a * comp_scale(T::comp(q));
+  }
+  double raw[3];
+  raw_from_vc(KIND, v, mf, raw);
+#pragma unroll
+  for (int r = 0; r < T::raw; ++r) rawrows[(long long)s * T::raw + r] = raw[r];
+}
+
 // ---------------------------------------------------------------------------
 // Background layers, one thread per station, layers in order (the running top
 // is accumulated exactly as the reference accumulates it).
@@ -148,6 +175,11 @@ __global__ void k_background(int kind, StationView st, int nbg, const double *__
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= st.n) return;
   const int raw = kind_raw(kind);
+  if (kind_special(kind)) {  // no background response (OMPMagneticGradImp.h:32-40)
+    for (int r = 0; r < raw; ++r)
+      for (int j = 0; j < nbg; ++j) bgsens[((long long)s * raw + r) * nbg + j] = 0.0;
+    return;
+  }
   const double mx = st.x[s], my = st.y[s], mz = st.z[s];
   double top = zo;
   for (int j = 0; j < nbg; ++j) {
@@ -276,8 +308,17 @@ __global__ void k_comp_weights(int kind, int nmeas, const double *__restrict__ w
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nmeas) return;
   const int raw = kind_raw(kind);
-  double w[10], u[NC_COUNT];
+  double w[10];
   for (int c = 0; c < raw; ++c) w[c] = w_raw[(long long)s * raw + c];
+  if (kind_special(kind)) {  // virtual-component weights [nmeas][ncomp]
+    const int nv = kind_ncomp(kind);
+    double u[kMaxVc];
+    vc_from_raw_weights(kind, w, mf, u);
+    for (int q = 0; q < nv; ++q)
+      W[(long long)s * nv + q] = u[q] * comp_scale(vc_comp(kind, q));
+    return;
+  }
+  double u[NC_COUNT];
   comps_from_raw_weights(kind, w, mf, u);
   for (int c = 0; c < NC_COUNT; ++c) W[(long long)s * NC_COUNT + c] = u[c] * comp_scale(c);
 }
@@ -291,9 +332,12 @@ template <int KIND>
 __global__ void __launch_bounds__(kThreads)
     k_node_adjoint(MeshView m, StationView st, const double *__restrict__ W, int spc,
                    double *__restrict__ Gpart) {
-  constexpr int MASK = KindTraits<KIND>::mask;
-  constexpr int NCMP = KindTraits<KIND>::ncomp;
-  constexpr int OFF = Slots<KIND>::off;
+  using T = KindTraits<KIND>;
+  constexpr int MASK = T::mask;
+  constexpr int NCMP = T::ncomp;
+  // weights: node-component layout [nmeas][NC_COUNT], or [nmeas][ncomp] for
+  // the special kinds
+  constexpr int WLD = T::special ? NCMP : NC_COUNT;
   const int ny1 = m.ny + 1, nz1 = m.nz + 1;
   const int nn = (m.nx + 1) * ny1 * nz1;
   const int n = blockIdx.x * kThreads + threadIdx.x;
@@ -305,7 +349,9 @@ __global__ void __launch_bounds__(kThreads)
   if (n < nn) decode_node(n, ny1, nz1, i, j, k);
   const double X = (n < nn) ? m.X[i] : 0.0, Y = (n < nn) ? m.Y[j] : 0.0,
                Z = (n < nn) ? m.Z[k] : 0.0;
-  double acc = 0.0;
+  double acc[T::nblock];
+#pragma unroll
+  for (int b = 0; b < T::nblock; ++b) acc[b] = 0.0;
   for (int base = s0; base < s1; base += kStage) {
     const int cnt = min(kStage, s1 - base);
     __syncthreads();
@@ -314,27 +360,36 @@ __global__ void __launch_bounds__(kThreads)
       sy[t] = st.y[base + t];
       sz[t] = st.z[base + t];
 #pragma unroll
-      for (int q = 0; q < NCMP; ++q) sw[t][q] = W[(long long)(base + t) * NC_COUNT + q + OFF];
+      for (int q = 0; q < NCMP; ++q)
+        sw[t][q] = W[(long long)(base + t) * WLD + (T::special ? q : T::comp(q))];
     }
     __syncthreads();
     if (n < nn) {
       for (int t = 0; t < cnt; ++t) {
-        double F[NC_COUNT];
-        node_terms<MASK>(sub(sx[t], X), sub(sy[t], Y), sub(sz[t], Z), F);
+        double F[T::twin ? 2 : 1][NC_COUNT];
+        const double dx = sub(sx[t], X), dy = sub(sy[t], Y);
+        node_terms<MASK>(dx, dy, sub(sz[t], Z), F[0]);
+        if constexpr (T::twin) node_terms<MASK>(dx, dy, sub(add(sz[t], 1.0), Z), F[T::twin ? 1 : 0]);
 #pragma unroll
-        for (int q = 0; q < NCMP; ++q) acc = fma(sw[t][q], F[q + OFF], acc);
+        for (int q = 0; q < NCMP; ++q)
+          acc[T::block(q)] = fma(sw[t][q], F[T::at(q)][T::comp(q)], acc[T::block(q)]);
       }
     }
   }
-  if (n < nn) Gpart[(long long)chunk * nn + n] = acc;
+  if (n < nn) {
+#pragma unroll
+    for (int b = 0; b < T::nblock; ++b)
+      Gpart[((long long)chunk * T::nblock + b) * nn + n] = acc[b];
+  }
 }
 
-__global__ void k_sum_chunks(int nn, int nchunk, const double *__restrict__ Gpart,
-                             double *__restrict__ G) {
+// G[n] = sum_c Gpart[c * stride + n] (stride = blocks x nodes per chunk).
+__global__ void k_sum_chunks(int nn, int nchunk, long long stride,
+                             const double *__restrict__ Gpart, double *__restrict__ G) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= nn) return;
   double v = 0.0;
-  for (int c = 0; c < nchunk; ++c) v += Gpart[(long long)c * nn + n];
+  for (int c = 0; c < nchunk; ++c) v += Gpart[(long long)c * stride + n];
   G[n] = v;
 }
 
@@ -382,9 +437,9 @@ __global__ void k_background_grad(int kind, int nmeas, int nbg, const double *__
 template <int KIND>
 __global__ void __launch_bounds__(kThreads)
     k_node_eval(MeshView m, StationView st, int s0, double *__restrict__ F) {
-  constexpr int MASK = KindTraits<KIND>::mask;
-  constexpr int NCMP = KindTraits<KIND>::ncomp;
-  constexpr int OFF = Slots<KIND>::off;
+  using T = KindTraits<KIND>;
+  constexpr int MASK = T::mask;
+  constexpr int NCMP = T::ncomp;
   const int ny1 = m.ny + 1, nz1 = m.nz + 1;
   const int nn = (m.nx + 1) * ny1 * nz1;
   const int n = blockIdx.x * kThreads + threadIdx.x;
@@ -393,20 +448,51 @@ __global__ void __launch_bounds__(kThreads)
   int i, j, k;
   decode_node(n, ny1, nz1, i, j, k);
   const int s = s0 + sl;
-  double v[NC_COUNT];
-  node_terms<MASK>(sub(st.x[s], m.X[i]), sub(st.y[s], m.Y[j]), sub(st.z[s], m.Z[k]), v);
+  double v[T::twin ? 2 : 1][NC_COUNT];
+  const double dx = sub(st.x[s], m.X[i]), dy = sub(st.y[s], m.Y[j]);
+  node_terms<MASK>(dx, dy, sub(st.z[s], m.Z[k]), v[0]);
+  if constexpr (T::twin) node_terms<MASK>(dx, dy, sub(add(st.z[s], 1.0), m.Z[k]), v[T::twin ? 1 : 0]);
 #pragma unroll
-  for (int q = 0; q < NCMP; ++q) F[((long long)sl * NCMP + q) * nn + n] = v[q + OFF];
+  for (int q = 0; q < NCMP; ++q) F[((long long)sl * NCMP + q) * nn + n] = v[T::at(q)][T::comp(q)];
+}
+
+// Raw rows of one cell from its virtual-component box values u[q]:
+// the ordinary kinds through raw_from_comps, the vertical gradient through
+// raw_from_vc (BzSensBot - BzSensTop, OMPMagneticGradImp.cpp:88-99) and
+// magnetisation as factor * U_kj in row k, column block j
+// (OMPMagnetizationImp.cpp:58-68, 93-104).
+template <int KIND>
+__device__ __forceinline__ void store_cell_rows(const double *u, const MagField &mf,
+                                                long long ngrid, long long cell, double *rows,
+                                                long long ld) {
+  using T = KindTraits<KIND>;
+  if constexpr (KIND == KIND_MAGNETIZATION) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int jb = 0; jb < 3; ++jb)
+        rows[(long long)k * ld + jb * ngrid + cell] = mul(mf.factor, u[3 * k + jb]);
+  } else if constexpr (KIND == KIND_MAG_GRADIENT) {
+    double raw[3];
+    raw_from_vc(KIND, u, mf, raw);
+    rows[cell] = raw[0];
+  } else {
+    double c[NC_COUNT];
+#pragma unroll
+    for (int q = 0; q < T::ncomp; ++q) c[T::comp(q)] = u[q];
+    double raw[10];
+    raw_from_comps(KIND, c, mf, raw);
+#pragma unroll
+    for (int r = 0; r < T::raw; ++r) rows[(long long)r * ld + cell] = raw[r];
+  }
 }
 
 template <int KIND>
 __global__ void __launch_bounds__(kThreads)
     k_cell_rows(MeshView m, const double *__restrict__ F, MagField mf, double *__restrict__ rows,
                 long long ld) {
-  constexpr int MASK = KindTraits<KIND>::mask;
-  constexpr int NCMP = KindTraits<KIND>::ncomp;
-  constexpr int OFF = Slots<KIND>::off;
-  constexpr int RAW = KindTraits<KIND>::raw;
+  using T = KindTraits<KIND>;
+  constexpr int NCMP = T::ncomp;
   const long long cell = (long long)blockIdx.x * kThreads + threadIdx.x;
   const int sl = blockIdx.y;
   if (cell >= m.ngrid()) return;
@@ -416,7 +502,7 @@ __global__ void __launch_bounds__(kThreads)
   const int i = t / m.ny;
   const int ny1 = m.ny + 1, nz1 = m.nz + 1;
   const int nn = (m.nx + 1) * ny1 * nz1;
-  double u[NC_COUNT];
+  double u[kMaxVc];
 #pragma unroll
   for (int q = 0; q < NCMP; ++q) {
     const double *f = F + ((long long)sl * NCMP + q) * nn;
@@ -424,13 +510,9 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
     for (int c = 0; c < 8; ++c)
       v[c] = f[((i + ((c >> 2) & 1)) * ny1 + (j + ((c >> 1) & 1))) * nz1 + (k + (c & 1))];
-    u[q + OFF] = combine8(q + OFF, v);
+    u[q] = combine8(T::comp(q), v);
   }
-  (void)MASK;
-  double raw[10];
-  raw_from_comps(KIND, u, mf, raw);
-#pragma unroll
-  for (int r = 0; r < RAW; ++r) rows[((long long)sl * RAW + r) * ld + cell] = raw[r];
+  store_cell_rows<KIND>(u, mf, m.ngrid(), cell, rows + (long long)sl * T::raw * ld, ld);
 }
 
 // Stored rows for the device-resident sensitivity: the node components of the
@@ -481,8 +563,8 @@ template <int KIND>
 __global__ void __launch_bounds__(kThreads)
     k_cell_direct(MeshView m, StationView st, int s0, MagField mf, double *__restrict__ rows,
                   long long ld) {
-  constexpr int MASK = KindTraits<KIND>::mask;
-  constexpr int RAW = KindTraits<KIND>::raw;
+  using T = KindTraits<KIND>;
+  constexpr int MASK = T::mask;
   const long long cell = (long long)blockIdx.x * kThreads + threadIdx.x;
   const int sl = blockIdx.y;
   if (cell >= m.ngrid()) return;
@@ -491,13 +573,16 @@ __global__ void __launch_bounds__(kThreads)
   const int j = t % m.ny;
   const int i = t / m.ny;
   const int s = s0 + sl;
-  double u[NC_COUNT];
+  double c[T::twin ? 2 : 1][NC_COUNT];
   prism_components(MASK, st.x[s], st.y[s], st.z[s], m.X[i], m.Y[j], m.Z[k], m.xs[i], m.ys[j],
-                   m.zs[k], u);
-  double raw[10];
-  raw_from_comps(KIND, u, mf, raw);
+                   m.zs[k], c[0]);
+  if constexpr (T::twin)
+    prism_components(MASK, st.x[s], st.y[s], add(st.z[s], 1.0), m.X[i], m.Y[j], m.Z[k], m.xs[i],
+                     m.ys[j], m.zs[k], c[T::twin ? 1 : 0]);
+  double u[kMaxVc];
 #pragma unroll
-  for (int r = 0; r < RAW; ++r) rows[((long long)sl * RAW + r) * ld + cell] = raw[r];
+  for (int q = 0; q < T::ncomp; ++q) u[q] = c[T::at(q)][T::comp(q)];
+  store_cell_rows<KIND>(u, mf, m.ngrid(), cell, rows + (long long)sl * T::raw * ld, ld);
 }
 
 __global__ void k_rows_dot(int raw, long long ngrid, const double *__restrict__ rows,
@@ -550,14 +635,22 @@ inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
 
 // ---------------------------------------------------------------------------
 // Launchers
-#define J3G_DISPATCH(kind, CALL)                        \
-  switch (kind) {                                      \
-    case KIND_SCALAR: { constexpr int K = KIND_SCALAR; CALL; } break;     \
-    case KIND_TENSOR: { constexpr int K = KIND_TENSOR; CALL; } break;     \
-    case KIND_MAGNETIC: { constexpr int K = KIND_MAGNETIC; CALL; } break; \
-    case KIND_JOINT: { constexpr int K = KIND_JOINT; CALL; } break;       \
-    default: return cudaErrorInvalidValue;             \
+#define J3G_DISPATCH4(kind, CALL, OTHER)                                     \
+  switch (kind) {                                                            \
+    case KIND_SCALAR: { constexpr int K = KIND_SCALAR; CALL; } break;        \
+    case KIND_TENSOR: { constexpr int K = KIND_TENSOR; CALL; } break;        \
+    case KIND_MAGNETIC: { constexpr int K = KIND_MAGNETIC; CALL; } break;    \
+    case KIND_JOINT: { constexpr int K = KIND_JOINT; CALL; } break;          \
+    OTHER                                                                    \
+    default: return cudaErrorInvalidValue;                                   \
   }
+// every kind
+#define J3G_DISPATCH(kind, CALL)                                                       \
+  J3G_DISPATCH4(kind, CALL,                                                            \
+                case KIND_MAG_GRADIENT: { constexpr int K = KIND_MAG_GRADIENT; CALL; } break; \
+                case KIND_MAGNETIZATION: { constexpr int K = KIND_MAGNETIZATION; CALL; } break;)
+// the kinds with a node-component layout (stored sensitivity, node reduce)
+#define J3G_DISPATCH_ORDINARY(kind, CALL) J3G_DISPATCH4(kind, CALL, )
 
 cudaError_t launch_rho_tilde(const MeshView &m, const double *rho, double *rho_t,
                              cudaStream_t st) {
@@ -575,9 +668,19 @@ cudaError_t launch_node_forward(int kind, const MeshView &m, const StationView &
 }
 
 cudaError_t launch_forward_reduce(int kind, int nmeas, int nblk, const double *partial,
-                                  double *comps, cudaStream_t st) {
+                                  const MagField &mf, double *comps, cudaStream_t st) {
+  if (kind == KIND_MAG_GRADIENT) {
+    k_forward_reduce_raw<KIND_MAG_GRADIENT><<<cdiv(nmeas, kThreads), kThreads, 0, st>>>(
+        nmeas, nblk, partial, mf, comps);
+    return cudaGetLastError();
+  }
+  if (kind == KIND_MAGNETIZATION) {
+    k_forward_reduce_raw<KIND_MAGNETIZATION><<<cdiv(nmeas, kThreads), kThreads, 0, st>>>(
+        nmeas, nblk, partial, mf, comps);
+    return cudaGetLastError();
+  }
   const int n = nmeas * NC_COUNT;
-  J3G_DISPATCH(kind, (k_forward_reduce<K><<<cdiv(n, kThreads), kThreads, 0, st>>>(nmeas, nblk, partial, comps)));
+  J3G_DISPATCH_ORDINARY(kind, (k_forward_reduce<K><<<cdiv(n, kThreads), kThreads, 0, st>>>(nmeas, nblk, partial, comps)));
   return cudaGetLastError();
 }
 
@@ -624,11 +727,15 @@ cudaError_t launch_node_adjoint(int kind, const MeshView &m, const StationView &
   return cudaGetLastError();
 }
 
-cudaError_t launch_adjoint_combine(const MeshView &m, int nchunk, const double *Gpart, double *G,
-                                   double *grad, cudaStream_t st) {
+cudaError_t launch_adjoint_combine(const MeshView &m, int nchunk, int nblock, const double *Gpart,
+                                   double *G, double *grad, cudaStream_t st) {
   const long long nn = m.nnodes();
-  k_sum_chunks<<<cdiv(nn, kThreads), kThreads, 0, st>>>((int)nn, nchunk, Gpart, G);
-  k_adjoint_combine<<<cdiv(m.ngrid(), kThreads), kThreads, 0, st>>>(m, G, grad);
+  for (int b = 0; b < nblock; ++b) {
+    k_sum_chunks<<<cdiv(nn, kThreads), kThreads, 0, st>>>((int)nn, nchunk, nblock * nn,
+                                                           Gpart + b * nn, G + b * nn);
+    k_adjoint_combine<<<cdiv(m.ngrid(), kThreads), kThreads, 0, st>>>(m, G + b * nn,
+                                                                      grad + b * m.ngrid());
+  }
   return cudaGetLastError();
 }
 
@@ -655,7 +762,7 @@ cudaError_t launch_sens_rows(int kind, bool node_exact, const MeshView &m, const
 }
 
 int stored_rows_per_station(int kind) {
-  return kind == KIND_MAGNETIC ? 3 : kind_ncomp(kind);
+  return kind_special(kind) ? 0 : kind == KIND_MAGNETIC ? 3 : kind_ncomp(kind);
 }
 
 cudaError_t launch_stored_rows(int kind, const MeshView &m, const StationView &s, int s0, int ns,
@@ -664,10 +771,10 @@ cudaError_t launch_stored_rows(int kind, const MeshView &m, const StationView &s
   dim3 g1(cdiv(m.nnodes(), kThreads), ns);
   dim3 g2(cdiv(m.ngrid(), kThreads), ns);
   if (rows64) {
-    J3G_DISPATCH(kind, (k_node_eval<K><<<g1, kThreads, 0, st>>>(m, s, s0, F),
+    J3G_DISPATCH_ORDINARY(kind, (k_node_eval<K><<<g1, kThreads, 0, st>>>(m, s, s0, F),
                         k_cell_stored<K, double><<<g2, kThreads, 0, st>>>(m, F, mf, rows64, ld)));
   } else {
-    J3G_DISPATCH(kind, (k_node_eval<K><<<g1, kThreads, 0, st>>>(m, s, s0, F),
+    J3G_DISPATCH_ORDINARY(kind, (k_node_eval<K><<<g1, kThreads, 0, st>>>(m, s, s0, F),
                         k_cell_stored<K, float><<<g2, kThreads, 0, st>>>(m, F, mf, rows32, ld)));
   }
   return cudaGetLastError();

@@ -27,16 +27,19 @@ struct StationView {
 
 // Forward, node formulation:  per station and component
 //   U_c(s) = scale_c * sum_nodes F_c(s, node) * rho~(node)
-// rho~ = third mixed backward difference of the zero-padded model.
+// rho~ = third mixed backward difference of the zero-padded model (one model
+// block; magnetisation runs it once per block into rho_t + block * nnodes).
 cudaError_t launch_rho_tilde(const MeshView &m, const double *rho, double *rho_t,
                              cudaStream_t st);
-// partial: [nblk][nmeas][ncomp]; returns nblk through *nblk_out.
+// partial: [nblk][nmeas][ncomp] virtual-component sums; rho_t holds one
+// nnodes block per model block of the kind.
 cudaError_t launch_node_forward(int kind, const MeshView &m, const StationView &s,
                                 const double *rho_t, double *partial, int nblk,
                                 int nodes_per_block, int stations_per_block, cudaStream_t st);
-// comps: [nmeas][NC_COUNT] node-component sums (scaled), unused comps zero.
+// comps: [nmeas][NC_COUNT] node-component sums (scaled), unused comps zero;
+// for the vertical gradient and magnetisation the raw rows [nmeas][raw].
 cudaError_t launch_forward_reduce(int kind, int nmeas, int nblk, const double *partial,
-                                  double *comps, cudaStream_t st);
+                                  const MagField &mf, double *comps, cudaStream_t st);
 
 // Background: bgsens[s][raw][j] for each layer j (GravityBackground.cpp:24-137,
 // OMPMagneticSusceptibilityImp.cpp:31-101).
@@ -54,25 +57,29 @@ cudaError_t launch_assemble(int kind, int transform, double t_bx, double t_by, d
 
 // Adjoint.  w_raw [nmeas][raw] are the raw-row weights (misfit already
 // back-projected through the transform).  W [nmeas][NC_COUNT] receives the
-// node-component weights with the component scale folded in.
+// node-component weights with the component scale folded in ([nmeas][ncomp]
+// virtual-component weights for the vertical gradient and magnetisation).
 cudaError_t launch_backproject(int kind, int transform, double t_bx, double t_by, double t_bz,
                                int nmeas, const double *misfit, const double *raw,
                                double *w_raw, cudaStream_t st);
 cudaError_t launch_comp_weights(int kind, int nmeas, const double *w_raw, const MagField &mf,
                                 double *W, cudaStream_t st);
-// Gpart [nchunk][nnodes] = sum over the chunk's stations of sum_c W * F_c.
+// Gpart [nchunk][nblock][nnodes] = sum over the chunk's stations of
+// sum_q W_q * F_q, per model block.
 cudaError_t launch_node_adjoint(int kind, const MeshView &m, const StationView &s,
                                 const double *W, int stations_per_chunk, int nchunk,
                                 double *Gpart, cudaStream_t st);
-// grad[cell] = 2 * sum_corners (-1)^shifts * sum_chunks Gpart[chunk][node]
-cudaError_t launch_adjoint_combine(const MeshView &m, int nchunk, const double *Gpart,
+// grad[b * ngrid + cell] = 2 * sum_corners (-1)^shifts * sum_chunks
+// Gpart[chunk][b][node] for each model block b; G: nblock * nnodes scratch.
+cudaError_t launch_adjoint_combine(const MeshView &m, int nchunk, int nblock, const double *Gpart,
                                    double *G, double *grad, cudaStream_t st);
 // grad[ngrid + j] = 2 * sum_s sum_r w_raw[s][r] * bgsens[s][r][j]
 cudaError_t launch_background_grad(int kind, int nmeas, int nbg, const double *w_raw,
                                    const double *bgsens, double *grad_bg, cudaStream_t st);
 
 // Sensitivity rows (reference per-cell order).  rows[(sl*raw + r) * ld + cell]
-// for stations s0 .. s0+ns-1 (sl = s - s0).  node_exact selects the node-term
+// for stations s0 .. s0+ns-1 (sl = s - s0); magnetisation rows carry the three
+// blocks at columns b * ngrid + cell.  node_exact selects the node-term
 // path (F scratch of ns * ncomp * nnodes doubles), otherwise eight corner
 // evaluations per cell.
 cudaError_t launch_sens_rows(int kind, bool node_exact, const MeshView &m,

@@ -17,7 +17,7 @@ import math
 import numpy as np
 
 SEEDS = {1: 101, 2: 102, 3: 103, 4: 104, 5: 105}
-SCALAR, TENSOR, MAGNETIC, JOINT = 1, 2, 3, 4
+SCALAR, TENSOR, MAGNETIC, JOINT, MAG_GRADIENT, MAGNETIZATION = 1, 2, 3, 4, 5, 6
 T_NONE, T_FTG_INVARIANT, T_TOTAL_FIELD, T_TFA = 0, 1, 2, 3
 # Config 1 and 3 have an infinite bottom background layer; an infinite sheet
 # term grows without bound with thickness, so it is replaced by this finite
@@ -56,6 +56,8 @@ class Survey:
 
     @property
     def nparm(self):
+        if self.kind == MAGNETIZATION:   # three cell blocks, no background parameters
+            return 3 * self.ngrid
         return self.ngrid + self.bg_thick.size
 
     def coords(self, axis):
@@ -69,7 +71,8 @@ class Survey:
 
     @property
     def raw(self):
-        return {SCALAR: 1, TENSOR: 9, MAGNETIC: 3, JOINT: 10}[self.kind]
+        return {SCALAR: 1, TENSOR: 9, MAGNETIC: 3, JOINT: 10, MAG_GRADIENT: 1,
+                MAGNETIZATION: 3}[self.kind]
 
     @property
     def dpm(self):

@@ -21,7 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libjif3d_ref_elements.so")
 
-SCALAR, TENSOR, MAGNETIC = 1, 2, 3
+SCALAR, TENSOR, MAGNETIC, MAG_GRADIENT, MAGNETIZATION = 1, 2, 3, 5, 6
 T_NONE, T_FTG_INVARIANT, T_TOTAL_FIELD, T_TFA = 0, 1, 2, 3
 GRAV_CONST = 6.67428e-11
 
@@ -109,7 +109,7 @@ def tensor_box(*args) -> np.ndarray:
 
 
 def raw_per_meas(kind: int) -> int:
-    return {SCALAR: 1, TENSOR: 9, MAGNETIC: 3}[kind]
+    return {SCALAR: 1, TENSOR: 9, MAGNETIC: 3, MAG_GRADIENT: 1, MAGNETIZATION: 3}[kind]
 
 
 class Problem:
@@ -141,6 +141,10 @@ class Problem:
 
     @property
     def nparm(self):
+        # magnetisation: three cell blocks, no background parameters
+        # (Magnetics/ThreeDMagnetizationModel.h:66-69)
+        if self.kind == MAGNETIZATION:
+            return 3 * self.ngrid
         return self.ngrid + len(self.bg)
 
     @property

@@ -27,7 +27,8 @@
 #define ORC_GRAV_CONST 6.67428e-11 /* Gravity/BasicGravElements.h:22 */
 #define ORC_PI 3.141592653589793238462643383279502884
 
-enum { ORC_SCALAR = 1, ORC_TENSOR = 2, ORC_MAGNETIC = 3 };
+enum { ORC_SCALAR = 1, ORC_TENSOR = 2, ORC_MAGNETIC = 3, ORC_MAG_GRADIENT = 5,
+       ORC_MAGNETIZATION = 6 };
 enum { ORC_T_NONE = 0, ORC_T_FTG_INVARIANT = 1, ORC_T_TOTAL_FIELD = 2, ORC_T_TFA = 3 };
 
 /* ---------------------------------------------------------------------------
@@ -174,7 +175,15 @@ typedef struct {
 
 static int raw_per_meas(int kind)
 {
-  return kind == ORC_SCALAR ? 1 : (kind == ORC_TENSOR ? 9 : 3);
+  return (kind == ORC_SCALAR || kind == ORC_MAG_GRADIENT) ? 1 : (kind == ORC_TENSOR ? 9 : 3);
+}
+
+/* Model parameters per cell block: three magnetisation components
+ * (Magnetics/ThreeDMagnetizationModel.h:53-70: x block, y block, z block,
+ * no background parameters), else one value per cell plus the background. */
+static size_t ncols_of(int kind, int ngrid, int nbg)
+{
+  return kind == ORC_MAGNETIZATION ? (size_t)3 * ngrid : (size_t)ngrid + nbg;
 }
 
 static int out_per_meas(const orc_problem *p)
@@ -195,10 +204,43 @@ static void mag_project(const orc_problem *p, const double *u, double *b)
   b[2] = (u[6] * bx + u[7] * by + u[8] * bz) * p->fs * factor;
 }
 
-/* Raw sensitivities of one cell for one station (1, 9 or 3 values). */
+/* z component of the field of one cell at (mx, my, mz) for the vertical
+ * gradient: Magnetics/OMPMagneticGradImp.cpp:20-22, 58-73 (factor 1e-7 / G). */
+static double grad_bz(const orc_problem *p, double mx, double my, double mz, int xi, int yi,
+                      int zi)
+{
+  const double bx = cos(p->inc) * cos(p->dec);
+  const double by = cos(p->inc) * sin(p->dec);
+  const double bz = sin(p->inc);
+  double u[9];
+  orc_tensor_box(mx, my, mz, p->xc[xi], p->yc[yi], p->zc[zi], p->xs[xi], p->ys[yi], p->zs[zi],
+                 u);
+  const double factor = 1e-7 / ORC_GRAV_CONST;
+  return (u[6] * bx + u[7] * by + u[8] * bz) * p->fs * factor;
+}
+
+/* Raw sensitivities of one cell for one station (1, 9 or 3 values; for the
+ * vertical gradient the two fields Bz(z) and Bz(z + 1), whose difference is
+ * the row; for magnetisation the 3 x 3 block factor * U, row-major). */
 static void cell_sens(const orc_problem *p, int s, int xi, int yi, int zi, double *out)
 {
   const double mx = p->mx[s], my = p->my[s], mz = p->mz[s];
+  if (p->kind == ORC_MAG_GRADIENT) {
+    out[0] = grad_bz(p, mx, my, mz, xi, yi, zi);       /* OMPMagneticGradImp.cpp:58-71 */
+    out[1] = grad_bz(p, mx, my, mz + 1, xi, yi, zi);   /* :76-86 */
+    return;
+  }
+  if (p->kind == ORC_MAGNETIZATION) {
+    /* Magnetics/OMPMagnetizationImp.cpp:58-68: currvalue = factor * U */
+    const double mag_mu = 4e-7 * ORC_PI;
+    const double factor = 1.0e9 * mag_mu / (4 * ORC_PI * ORC_GRAV_CONST);
+    double u[9];
+    orc_tensor_box(mx, my, mz, p->xc[xi], p->yc[yi], p->zc[zi], p->xs[xi], p->ys[yi],
+                   p->zs[zi], u);
+    for (int c = 0; c < 9; ++c)
+      out[c] = factor * u[c];
+    return;
+  }
   if (p->kind == ORC_SCALAR) {
     out[0] = orc_grav_box(mx, my, mz, p->xc[xi], p->yc[yi], p->zc[zi], p->xs[xi],
                           p->ys[yi], p->zs[zi]);
@@ -220,11 +262,38 @@ static void cell_sens(const orc_problem *p, int s, int xi, int yi, int zi, doubl
  * the sum is taken in offset order; with more, OpenMP splits it in contiguous
  * chunks and adds the chunk sums (the reference's reduction(+)).
  * sens: raw x ncol row-major (ncol >= ngrid) or NULL. */
+/* Per-cell accumulation of the two new kinds (into acc[0..2]) and their rows.
+ * Vertical gradient: BzBot += BzSensBot * chi, BzTop += BzSensTop * chi, row
+ * BzSensBot - BzSensTop (OMPMagneticGradImp.cpp:71-100).  Magnetisation:
+ * B_k += (c_k0 mx + c_k1 my) + c_k2 mz, rows c_kj at column offset + j*ngrid
+ * (OMPMagnetizationImp.cpp:70-104). */
+static void accumulate_special(const orc_problem *p, const double *v, const double *model,
+                               int offset, int ngrid, double *acc, double *sens, size_t ncol)
+{
+  if (p->kind == ORC_MAG_GRADIENT) {
+    const double chi = model[offset];
+    acc[0] += v[0] * chi;
+    acc[1] += v[1] * chi;
+    if (sens)
+      sens[offset] = v[0] - v[1];
+    return;
+  }
+  const double m0 = model[offset], m1 = model[offset + ngrid], m2 = model[offset + 2 * ngrid];
+  for (int k = 0; k < 3; ++k) {
+    acc[k] += (v[3 * k] * m0 + v[3 * k + 1] * m1 + v[3 * k + 2] * m2);
+    if (sens)
+      for (int j = 0; j < 3; ++j)
+        sens[(size_t)k * ncol + offset + (size_t)j * ngrid] = v[3 * k + j];
+  }
+}
+
 static void gridded(const orc_problem *p, int s, const double *model, double *result,
                     double *sens, size_t ncol)
 {
   const int ngrid = p->nx * p->ny * p->nz;
   const int raw = raw_per_meas(p->kind);
+  const int special = p->kind == ORC_MAG_GRADIENT || p->kind == ORC_MAGNETIZATION;
+  const int nacc = p->kind == ORC_MAG_GRADIENT ? 2 : raw;
   double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 #ifdef _OPENMP
 #pragma omp parallel num_threads(p->nthreads > 0 ? p->nthreads : 1)
@@ -238,6 +307,10 @@ static void gridded(const orc_problem *p, int s, const double *model, double *re
       const int xi = rest / p->ny;
       double v[9];
       cell_sens(p, s, xi, yi, zi, v);
+      if (special) {
+        accumulate_special(p, v, model, offset, ngrid, local, sens, ncol);
+        continue;
+      }
       const double rho = model[offset];
       for (int c = 0; c < raw; ++c) {
         local[c] += v[c] * rho;
@@ -248,7 +321,7 @@ static void gridded(const orc_problem *p, int s, const double *model, double *re
 #pragma omp for ordered schedule(static, 1)
     for (int t = 0; t < omp_get_num_threads(); ++t) {
 #pragma omp ordered
-      for (int c = 0; c < raw; ++c)
+      for (int c = 0; c < nacc; ++c)
         acc[c] += local[c];
     }
   }
@@ -260,6 +333,10 @@ static void gridded(const orc_problem *p, int s, const double *model, double *re
     const int xi = rest / p->ny;
     double v[9];
     cell_sens(p, s, xi, yi, zi, v);
+    if (special) {
+      accumulate_special(p, v, model, offset, ngrid, acc, sens, ncol);
+      continue;
+    }
     const double rho = model[offset];
     for (int c = 0; c < raw; ++c) {
       acc[c] += v[c] * rho;
@@ -268,6 +345,10 @@ static void gridded(const orc_problem *p, int s, const double *model, double *re
     }
   }
 #endif
+  if (p->kind == ORC_MAG_GRADIENT) {
+    result[0] = acc[0] - acc[1]; /* returnvalue(0) = BzBot - BzTop */
+    return;
+  }
   for (int c = 0; c < raw; ++c)
     result[c] = acc[c];
 }
@@ -281,6 +362,16 @@ static void background(const orc_problem *p, int s, double xw, double yw, double
                        int ngrid)
 {
   const int raw = raw_per_meas(p->kind);
+  if (p->kind == ORC_MAG_GRADIENT || p->kind == ORC_MAGNETIZATION) {
+    /* no background response: OMPMagneticGradImp.h:32-40, OMPMagnetizationImp.cpp:16-22
+     * (the gradient's background columns stay zero; magnetisation has none) */
+    for (int c = 0; c < raw; ++c)
+      result[c] = 0.0;
+    if (sens && p->kind == ORC_MAG_GRADIENT)
+      for (int j = 0; j < p->nbg; ++j)
+        sens[(size_t)ngrid + j] = 0.0;
+    return;
+  }
   const double mx = p->mx[s], my = p->my[s], mz = p->mz[s];
   double top = p->zc[0];
   double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -420,7 +511,7 @@ int orc_forward(int nx, int ny, int nz, const double *xc, const double *yc, cons
   orc_problem p = make_problem(nx, ny, nz, xc, yc, zc, xs, ys, zs, nbg, bg_thick, nmeas, mx,
                                my, mz, kind, inc, dec, fs, transform, t_inc, t_dec, nthreads);
   const int ngrid = nx * ny * nz;
-  const size_t ncol = (size_t)ngrid + nbg;
+  const size_t ncol = ncols_of(kind, ngrid, nbg);
   const int raw = raw_per_meas(kind);
   const int dpm = out_per_meas(&p);
   const double xw = width_sum(xs, nx), yw = width_sum(ys, ny), zw = width_sum(zs, nz);
@@ -452,7 +543,7 @@ int orc_lqderivative(int nx, int ny, int nz, const double *xc, const double *yc,
   orc_problem p = make_problem(nx, ny, nz, xc, yc, zc, xs, ys, zs, nbg, bg_thick, nmeas, mx,
                                my, mz, kind, inc, dec, fs, transform, t_inc, t_dec, nthreads);
   const int ngrid = nx * ny * nz;
-  const size_t ncol = (size_t)ngrid + nbg;
+  const size_t ncol = ncols_of(kind, ngrid, nbg);
   const int raw = raw_per_meas(kind);
   const int dpm = out_per_meas(&p);
   const double xw = width_sum(xs, nx), yw = width_sum(ys, ny), zw = width_sum(zs, nz);

@@ -273,3 +273,85 @@ def test_openmp_thread_count_invariance(oracle_lib):
     p.nthreads = 1
     d2 = p.forward(s.model)
     np.testing.assert_allclose(d1, d2, rtol=1e-12, atol=1e-22)
+
+
+def magnetization_survey(seed, nx=4, ny=3, nz=3, nmeas=3, transform=W.T_NONE):
+    """Small magnetisation survey: three cell blocks, no background."""
+    s = small_survey(W.MAGNETIZATION, nx=nx, ny=ny, nz=nz, nmeas=nmeas, seed=seed, bg=False,
+                     transform=transform)
+    rng = np.random.default_rng(seed + 1000)
+    s.model = rng.uniform(0.1, 2.0, 3 * s.ngrid)
+    return s
+
+
+@pytest.mark.parametrize("kind", [W.MAG_GRADIENT, W.MAGNETIZATION])
+def test_objective_fd_gradient_magnetic_kinds(oracle_lib, kind):
+    """Objective gradient vs central differences for the vertical magnetic
+    gradient (test_MagneticGradObjective.cpp:72-110) and magnetisation
+    (test_MagneticObjective.cpp:176-211), step 1 %, 0.01 %."""
+    O = oracle_lib
+    s = (magnetization_survey(31) if kind == W.MAGNETIZATION
+         else small_survey(kind, nx=4, ny=3, nz=3, nmeas=3, seed=31, bg=False))
+    obs = oracle_problem(O, s).forward(s.model) * 1.1
+    sigma2 = np.ones_like(obs)
+    _, d = objective(O, s, s.model, obs, sigma2)
+    grad = oracle_problem(O, s).lqderivative(s.model, (d - obs) / sigma2)
+    for i in range(s.model.size):
+        delta = s.model[i] * 0.01
+        mp, mm = s.model.copy(), s.model.copy()
+        mp[i] += delta
+        mm[i] -= delta
+        fd = (objective(O, s, mp, obs, sigma2)[0] - objective(O, s, mm, obs, sigma2)[0]) / (2 * delta)
+        check_close(fd, grad[i], 0.01)
+
+
+def test_magnetization_equals_induced(oracle_lib):
+    """Magnetisation M = chi F b / (1e9 mu0) reproduces the induced field of
+    the susceptibility chi (the two implementations share the tensor terms:
+    OMPMagnetizationImp.cpp:58-68 vs OMPMagneticSusceptibilityImp.cpp:116-170)."""
+    O = oracle_lib
+    s = small_survey(W.MAGNETIC, seed=33, bg=False)
+    chi = s.model[:s.ngrid]
+    b = np.array([math.cos(s.inc) * math.cos(s.dec), math.cos(s.inc) * math.sin(s.dec),
+                  math.sin(s.inc)])
+    mu0 = 4e-7 * math.pi
+    ref = oracle_problem(O, s).forward(chi)
+    m = magnetization_survey(33)
+    m.xsize, m.ysize, m.zsize, m.stations = s.xsize, s.ysize, s.zsize, s.stations
+    m.origin = s.origin
+    model = np.concatenate([chi * s.fs * b[j] / (1e9 * mu0) for j in range(3)])
+    got = oracle_problem(O, m).forward(model)
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+
+
+def test_vertical_gradient_is_field_difference(oracle_lib):
+    """Bz(z) - Bz(z + 1 m) of OMPMagneticGradImp equals the difference of the
+    magnetic Bz rows at the two heights times mu0 (its factor 1e-7 / G
+    against 1 / (4 pi G)); background layers contribute nothing."""
+    O = oracle_lib
+    s = small_survey(W.MAG_GRADIENT, seed=35, bg=True)
+    got = oracle_problem(O, s).forward(s.model)
+    m = small_survey(W.MAGNETIC, seed=35, bg=False)
+    chi = s.model[:s.ngrid]
+    top = m.subset(np.arange(s.stations.shape[0]))
+    top.stations = s.stations + np.array([0.0, 0.0, 1.0])
+    bz0 = oracle_problem(O, m).forward(chi).reshape(-1, 3)[:, 2]
+    bz1 = oracle_problem(O, top).forward(chi).reshape(-1, 3)[:, 2]
+    ref = (bz0 - bz1) * 4e-7 * math.pi
+    np.testing.assert_allclose(got, ref, rtol=1e-9, atol=1e-9 * np.abs(ref).max())
+    # the background columns of the sensitivity are zero
+    _, J = oracle_problem(O, s).forward(s.model, True)
+    assert J.shape == (s.stations.shape[0], s.nparm)
+    assert np.all(J[:, s.ngrid:] == 0.0)
+
+
+def test_lqderivative_equals_2JTr_magnetic_kinds(oracle_lib):
+    O = oracle_lib
+    for s in (small_survey(W.MAG_GRADIENT, seed=37), magnetization_survey(37, nx=5, ny=4, nz=3,
+                                                                          nmeas=6)):
+        p = oracle_problem(O, s)
+        r = np.random.default_rng(2).uniform(-1, 1, s.stations.shape[0] * s.raw)
+        g = p.lqderivative(s.model, r)
+        _, J = p.forward(s.model, True)
+        ref = O.sens_rmatvec2(J, r)
+        np.testing.assert_allclose(g, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
