@@ -150,6 +150,47 @@ class ThreeDSusceptibilityModel(ThreeDModelBase):
     GetBackgroundSusceptibilities = ThreeDModelBase.GetBackgroundValues
 
 
+class ThreeDMagnetizationModel(ThreeDModelBase):
+    """Remanent magnetisation: three cell arrays, model parameters x block, y
+    block, z block and no background parameters
+    (Magnetics/ThreeDMagnetizationModel.h:53-70)."""
+
+    def __init__(self):
+        super().__init__()
+        self._my = np.zeros((0, 0, 0))
+        self._mz = np.zeros((0, 0, 0))
+
+    def SetMeshSize(self, nx, ny, nz):
+        super().SetMeshSize(nx, ny, nz)
+        self._my = np.zeros((nx, ny, nz))
+        self._mz = np.zeros((nx, ny, nz))
+
+    def SetMagnetization_X(self):
+        return self._data
+
+    def GetMagnetization_X(self):
+        return self._data
+
+    def SetMagnetization_Y(self):
+        return self._my
+
+    def GetMagnetization_Y(self):
+        return self._my
+
+    def SetMagnetization_Z(self):
+        return self._mz
+
+    def GetMagnetization_Z(self):
+        return self._mz
+
+    def GetModelParameters(self):
+        return np.concatenate([self._data.reshape(-1), self._my.reshape(-1),
+                               self._mz.reshape(-1)])
+
+    def GetNModelParm(self):
+        return 3 * self._data.size
+
+
 class GeneralData:
     """Measurement positions (DataBase/GeneralData.h)."""
 
@@ -187,6 +228,10 @@ class TensorGravityData(GeneralData):
 
 class TotalFieldMagneticData(GeneralData):
     ModelType = ThreeDSusceptibilityModel
+
+
+class ThreeComponentMagneticData(GeneralData):
+    ModelType = ThreeDMagnetizationModel
 
 
 # ---------------------------------------------------------------------------
@@ -294,7 +339,8 @@ class GB300GravMagImplementation:
         return self._ctx
 
     def RawDataPerMeasurement(self):
-        return {capi.SCALAR: 1, capi.TENSOR: 9, capi.MAGNETIC: 3, capi.JOINT: 10}[self.KIND]
+        return {capi.SCALAR: 1, capi.TENSOR: 9, capi.MAGNETIC: 3, capi.JOINT: 10,
+                capi.MAG_GRADIENT: 1, capi.MAGNETIZATION: 3}[self.KIND]
 
     def SetDataTransform(self, transform):
         self.Transform = transform
@@ -382,6 +428,22 @@ class GB300MagneticSusceptibilityImp(GB300GravMagImplementation):
 
     def _kind_args(self):
         return (self.KIND, self.Inclination, self.Declination, self.FieldStrength)
+
+
+class GB300MagneticGradImp(GB300MagneticSusceptibilityImp):
+    """Replaces OMPMagneticGradImp (Magnetics/OMPMagneticGradImp.h:20-64): one
+    datum per station, the vertical gradient Bz(z) - Bz(z + 1 m); background
+    layers do not respond."""
+    KIND = capi.MAG_GRADIENT
+
+    def __init__(self, Inc=0.0, Dec=0.0, Fs=1.0, device=0):
+        super().__init__(Inc, Dec, Fs, device)
+
+
+class GB300MagnetizationImp(GB300GravMagImplementation):
+    """Replaces OMPMagnetizationImp (Magnetics/OMPMagnetizationImp.h:20-50):
+    Bx, By, Bz of a ThreeDMagnetizationModel (no inducing-field parameters)."""
+    KIND = capi.MAGNETIZATION
 
 
 # ---------------------------------------------------------------------------
@@ -538,3 +600,68 @@ class FullSensitivityGravMagCalculator(CachedGravMagCalculator):
                 processed[o:o + nin] = self.Transform.Derivative(result[o:o + nin]).T @ \
                     misfit[i:i + nout]
         return 2.0 * (self.Sensitivities.T @ processed)
+
+
+class DeviceSensitivityGravMagCalculator(ThreeDGravMagCalculator):
+    """GPU twin of FullSensitivity / CachedGravMagCalculator
+    (GravMag/FullSensitivityGravMagCalculator.h:33-221,
+    GravMag/CachedGravMagCalculator.h:28-143): the first call on a geometry
+    computes the data in FP64 and builds the sensitivity matrix in HBM
+    (j3g_build_sensitivity); later calls on the same geometry run the stored
+    products on the device (FP32 streaming or fp16 hi/lo tensor-core,
+    relative error <= 1e-6) instead of recomputing box terms.
+
+    The cache key is the full geometry -- cell sizes, origin, background
+    thicknesses, the station positions (which the reference's
+    GridBackgroundModelCache omits) and the kind / transform -- and not the
+    model values, which J does not depend on.
+    """
+
+    def __init__(self, imp, storage=capi.STORE_FP32):
+        super().__init__(imp)
+        self.storage = storage
+        self._key = None
+
+    def InvalidateCache(self):
+        self._key = None
+
+    def _geometry_key(self, Model, Data):
+        t = self.Imp.Transform
+        return (self.Imp._kind_args(), t.code if t else 0, getattr(t, "inclination", 0.0),
+                getattr(t, "declination", 0.0),
+                Model.GetXOrigin(), Model.GetYOrigin(), Model.GetZOrigin(),
+                Model.GetXCellSizes().tobytes(), Model.GetYCellSizes().tobytes(),
+                Model.GetZCellSizes().tobytes(), Model.GetBackgroundThicknesses().tobytes(),
+                Data.GetMeasPosX().tobytes(), Data.GetMeasPosY().tobytes(),
+                Data.GetMeasPosZ().tobytes())
+
+    def _cached(self, Model, Data):
+        """(context, True) on a cache hit, else (context, the new key)."""
+        key = self._geometry_key(Model, Data)
+        ctx = self.Imp._prepare(Model, Data)
+        if key == self._key and ctx.sensitivity_info()["storage"] == self.storage:
+            return ctx, True
+        return ctx, key
+
+    def Calculate(self, Model, Data):
+        self.CheckModelConsistency(Model)
+        ctx, hit = self._cached(Model, Data)
+        model = Model.GetModelParameters()
+        if hit is True:
+            return ctx.batched_forward(model[None, :])[0]
+        data = ctx.forward(model)  # FP64, as the first call of the reference
+        ctx.build_sensitivity(self.storage)
+        self._key = hit
+        return data
+
+    def LQDerivative(self, Model, Data, Misfit):
+        self.CheckModelConsistency(Model)
+        ctx, hit = self._cached(Model, Data)
+        model = Model.GetModelParameters()
+        misfit = np.asarray(Misfit, dtype=float)
+        if hit is True:
+            return ctx.batched_lqderivative(model[None, :], misfit[None, :])[0]
+        return ctx.lqderivative(model, misfit)
+
+    def HandleSensitivities(self, measindex):
+        pass
