@@ -68,3 +68,19 @@ def test_null_context_is_rejected(lib):
     lib.j3g_forward.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     assert lib.j3g_forward(None, None, None) == 1
     assert lib.j3g_destroy(None) == 0
+
+
+def test_cpp_implementation_header_compiles():
+    """The C++ implementation objects compile against the stand-in jif3D
+    declarations (no GPU needed: syntax and template instantiation only)."""
+    import shutil
+    import subprocess
+    if not shutil.which("g++"):
+        pytest.skip("g++ not available")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror",
+                        "-I", os.path.join(root, "include"),
+                        "-I", os.path.join(root, "jif3d_gb300", "host"),
+                        os.path.join(root, "tests", "cpp", "host_adapter_check.cpp")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
