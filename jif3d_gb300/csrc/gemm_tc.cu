@@ -30,6 +30,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
+#include <set>
+#include <utility>
 
 #include "stored.h"
 
@@ -747,6 +750,22 @@ bool make_tiled_map(CUtensorMap *map, const void *base, long long rows, long lon
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Dynamic shared-memory opt-in of a kernel, once per kernel and device: the
+// launchers stay free of non-stream CUDA calls after the first launch, so a
+// caller can capture later launches in a CUDA graph.
+cudaError_t allow_smem_once(const void *kernel, int bytes) {
+  static std::mutex mu;
+  static std::set<std::pair<const void *, int>> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count({kernel, dev})) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) done.insert({kernel, dev});
+  return e;
+}
+
 template <int BN, bool F16>
 cudaError_t launch_bn(const GemmOperands &g, int nsplit, float *P, long long ldp, long long slice,
                       int *err, cudaStream_t st) {
@@ -758,9 +777,8 @@ cudaError_t launch_bn(const GemmOperands &g, int nsplit, float *P, long long ldp
   const int kb_total = (int)(g.ld / BK);
   const int kb_per = (kb_total + nsplit - 1) / nsplit;
   const int nsp = (kb_total + kb_per - 1) / kb_per;
-  cudaError_t e = cudaFuncSetAttribute(k_gemm_x3<BN, F16>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       Cfg<BN, F16>::SMEM);
+  cudaError_t e = allow_smem_once(reinterpret_cast<const void *>(k_gemm_x3<BN, F16>),
+                                  Cfg<BN, F16>::SMEM);
   if (e != cudaSuccess) return e;
   // N tiles vary fastest so the CTAs sharing an A tile run side by side (L2 reuse)
   dim3 grid((unsigned)(g.n_pad / BN), (unsigned)((g.m + BM - 1) / BM), (unsigned)nsp);
@@ -780,9 +798,8 @@ cudaError_t launch_pair(const GemmOperands &g, int nsplit, float *P, long long l
   const int kb_total = (int)(g.ld / BK);
   const int kb_per = (kb_total + nsplit - 1) / nsplit;
   const int nsp = (kb_total + kb_per - 1) / kb_per;
-  cudaError_t e = cudaFuncSetAttribute(k_gemm_pair<F16>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       PairCfg<F16>::SMEM);
+  cudaError_t e = allow_smem_once(reinterpret_cast<const void *>(k_gemm_pair<F16>),
+                                  PairCfg<F16>::SMEM);
   if (e != cudaSuccess) return e;
   // x: CTA pairs over M (two CTAs of 128 rows each), y: N tiles of 256, z: K splits
   dim3 grid((unsigned)(2 * ((g.m + 255) / 256)), (unsigned)(g.n_pad / kPairN), (unsigned)nsp);
