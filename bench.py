@@ -62,32 +62,57 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled during the timed region:
+    start() returns once nvidia-smi is printing (so sampling covers the region
+    from its first step), samples come every 10 ms and only those read between
+    start() and stop() count."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index):
+    def __init__(self, index, period_ms=10):
         self.index = index
+        self.period_ms = period_ms
         self.proc = None
+        self.lines = []
+        self.counting = False
+
+    def _reader(self):
+        for line in self.proc.stdout:
+            if self.counting:
+                self.lines.append(line)
+            else:
+                self.first.set()
 
     def start(self):
+        import threading
+        self.first = threading.Event()
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-i", str(self.index), "-lms", "200"],
+                 "-i", str(self.index), "-lms", str(self.period_ms)],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
+            return
+        self.thread = threading.Thread(target=self._reader, daemon=True)
+        self.thread.start()
+        self.first.wait(timeout=15)
+        self.counting = True
 
     def stop(self):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.counting = False
+        lines = list(self.lines)
         self.proc.terminate()
-        out, _ = self.proc.communicate(timeout=10)
+        try:
+            self.proc.wait(timeout=10)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
         sm, smax, power, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in out.strip().splitlines():
+        for line in lines:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -102,7 +127,8 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
-                "power_w_max": max(power) if power else None, "samples": len(sm)}
+                "power_w_max": max(power) if power else None, "samples": len(sm),
+                "period_ms": self.period_ms}
 
 
 def measured_peaks():
@@ -191,6 +217,7 @@ def run_batched(args, rank, world, local):
     build_ms = e0.elapsed_time(e1)
     info = ctx.sensitivity_info()
 
+    ctx.set_autotune(True)  # first products of each shape pick their plan (warm-up)
     models = torch.tensor(s.models, dtype=torch.float64, device=dev)
     data = torch.zeros((nmod, n * 10), dtype=torch.float64, device=dev)
     misfit = torch.zeros_like(data)
@@ -312,6 +339,8 @@ def run_batched(args, rank, world, local):
             "peak_source": f"{src} bf16_tflops (burst; fp16 MMA runs at the bf16 rate)",
             "kernel": "k_gemm_pair<fp16> (CTA pair, 256 x 256 tiles, 3 fp16 products per launch)",
             "ms_per_launch": {"forward": gf_ms / max(1, gf_n), "adjoint": ga_ms / max(1, ga_n)},
+            "plans": {"forward": ctx.gemm_plan(0), "adjoint": ctx.gemm_plan(1),
+                      "how": "autotuned on the first call of each shape (K splits, N tile)"},
             "hbm_gbs_of_J_stream": j_bytes / (gemm_ms * 1e-3) / 1e9,
             "hbm_peak_gbs": peaks["hbm_gbs"]}
     ctx.close()

@@ -202,6 +202,23 @@ enum j3g_timer {
 int j3g_set_timing(j3g_context *ctx, int enable);
 int j3g_get_timing(j3g_context *ctx, int category, double *total_ms, long long *launches);
 
+/* Autotuning of the tensor-core products (J3G_STORE_F16X2 batched calls); no
+ * reference counterpart.  Off by default: a fixed rule picks the K-split count
+ * and the N tile.  With enable = 1, the first product of each shape (direction,
+ * rows, models, K) times a few candidate plans -- split counts that fill the
+ * last wave of CTAs, and one-SM 128-wide tiles in place of CTA pairs -- and
+ * keeps the fastest for the context's lifetime.  Every candidate keeps the
+ * accuracy bound of the fixed rule (at most 64 k-blocks per split).  Tuning
+ * synchronises the context's stream, so the first call of a shape must not be
+ * made while the stream is being captured into a CUDA graph; results can
+ * differ from the fixed plan's in the last bits (another summation order). */
+int j3g_set_autotune(j3g_context *ctx, int enable);
+/* The plan the last batched product used: direction 0 forward (J M), 1
+ * adjoint (J^T R); K splits requested, N tile (64, 128 or 256 = CTA pair) and
+ * the autotuner's time of that plan in ms (0 for the fixed rule). */
+int j3g_get_gemm_plan(const j3g_context *ctx, int direction, int *nsplit, int *tile,
+                      double *tuned_ms);
+
 /* Allocation-free gridded forward, for callers that cannot let a library
  * allocate device memory: hosts that reserve all device memory for their own
  * pool allocator at start-up, or loops that must not take the device-wide

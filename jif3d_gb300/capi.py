@@ -59,6 +59,8 @@ SIGNATURES = {
     "j3g_launch_count": (_I, [_VP, ctypes.POINTER(_LL)]),
     "j3g_set_timing": (_I, [_VP, _I]),
     "j3g_get_timing": (_I, [_VP, _I, _P, ctypes.POINTER(_LL)]),
+    "j3g_set_autotune": (_I, [_VP, _I]),
+    "j3g_get_gemm_plan": (_I, [_VP, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), _P]),
     "j3g_probe_fp64": (_I, [_VP, _P]),
     "j3g_probe_math": (_I, [_I, _I]),
     "j3g_forward_noalloc": (_I, [_I, _I, _I, _I, _VP, _VP, _VP, _I, _VP, _VP, _VP, _D, _D, _D,
@@ -256,6 +258,15 @@ class Context:
         self._check(self._lib.j3g_batched_lqderivative(self._h, m.shape[0], _ptr(m), _ptr(r),
                                                        _ptr(g)))
         return g
+
+    def set_autotune(self, enable=True):
+        self._check(self._lib.j3g_set_autotune(self._h, 1 if enable else 0))
+
+    def gemm_plan(self, direction):
+        ns, tile, ms = _I(), _I(), _D()
+        self._check(self._lib.j3g_get_gemm_plan(self._h, int(direction), ctypes.byref(ns),
+                                                ctypes.byref(tile), ctypes.byref(ms)))
+        return dict(nsplit=ns.value, tile=tile.value, tuned_ms=ms.value)
 
     def set_timing(self, enable=True):
         self._check(self._lib.j3g_set_timing(self._h, 1 if enable else 0))

@@ -13,6 +13,8 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <array>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -66,6 +68,16 @@ struct j3g_context {
   long long st_ldT = 0;        // rows padded to a multiple of 64 (transposed copy)
   DevBuf J32, Jhi, Jlo, JThi, JTlo, rowscale, Jrowsum;
   DevBuf x32, sums, part, Bhi, Blo, P, wst, wrawb, rawb, gerr, mscale, mmean, swork;
+
+  // tensor-core product plans (j3g_set_autotune): key direction, rows, padded
+  // models, K; the plan last used per direction is kept for j3g_get_gemm_plan
+  struct GemmPlan {
+    int nsplit = 0, tile = 0;
+    float ms = 0.0f;  // timed by the autotuner (0 for the fixed rule)
+  };
+  bool autotune = false;
+  std::map<std::array<long long, 4>, GemmPlan> plans;
+  GemmPlan last_plan[2];
 
   // optional per-category kernel timing (j3g_set_timing): event pairs
   // recorded on the context's stream around the dominant launches
@@ -611,6 +623,91 @@ int choose_splits(long long m, int ntiles, long long ld) {
   return (int)std::max<long long>(1, std::min(s, kb));
 }
 
+// Plan of one tensor-core product (K splits and N tile), with the partial-sum
+// buffer c->P sized for it.  Without autotuning, the fixed rule: choose_splits
+// and gemm_n_tile.  With autotuning, the first product of a shape times each
+// candidate -- the fixed plan, split counts that fill the last wave of CTAs on
+// the SMs, and one-SM 128-wide tiles where the pair kernel would run -- once
+// after an untimed run (CUDA events on the context's stream), keeps the
+// fastest for the context's lifetime and reuses it.  Every candidate keeps at
+// most 64 k-blocks per split, the bound that holds the FP32 register sums to
+// their accuracy.
+int gemm_plan(j3g_context *c, int dir, const GemmOperands &g, long long ldp, long long slice,
+              j3g_context::GemmPlan &plan) {
+  const int tile0 = gemm_n_tile((int)g.n);
+  plan.tile = tile0;
+  plan.nsplit = choose_splits(g.m, (int)(g.n_pad / tile0), g.ld);
+  plan.ms = 0.0f;
+  const std::array<long long, 4> key{dir, g.m, g.n_pad, g.ld};
+  auto it = c->autotune ? c->plans.find(key) : c->plans.end();
+  if (!c->autotune || it != c->plans.end()) {
+    if (it != c->plans.end()) plan = it->second;
+    return ensure(c, c->P, sizeof(float) * (size_t)gemm_splits_used(g.ld, plan.nsplit) * slice);
+  }
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  const long long kb = g.ld / 64, smin = (kb + 63) / 64;
+  std::vector<std::pair<int, int>> cand;  // (tile, nsplit)
+  for (int tile : {tile0, tile0 == 256 ? 128 : 0}) {
+    if (!tile || g.n_pad % tile) continue;
+    const int base = choose_splits(g.m, (int)(g.n_pad / tile), g.ld);
+    const long long smax = std::min<long long>(kb, 4LL * base);
+    cand.push_back({tile, base});
+    // CTAs per split: 128-row tiles (a pair counts two) x N tiles; one CTA per SM
+    const long long per = (tile == 256 ? 2 * ((g.m + 255) / 256) : (g.m + 127) / 128) *
+                          (g.n_pad / tile);
+    int added = 0;
+    for (long long w = 1; w <= 256 && added < 3; ++w) {
+      const long long s = w * sms / per;
+      if (s < std::max<long long>(smin, base) || s > smax) continue;
+      const int used = gemm_splits_used(g.ld, (int)s);
+      const long long rem = (long long)used * per % sms;
+      if (rem > sms / 10 && rem < sms * 9 / 10) continue;  // much of the last wave idle
+      bool seen = false;
+      for (auto &p : cand) seen |= (p.first == tile && gemm_splits_used(g.ld, p.second) == used);
+      if (!seen) {
+        cand.push_back({tile, (int)s});
+        ++added;
+      }
+    }
+  }
+  int nsp_max = 1;
+  for (auto &p : cand) nsp_max = std::max(nsp_max, gemm_splits_used(g.ld, p.second));
+  J3G_TRY(ensure(c, c->P, sizeof(float) * (size_t)nsp_max * slice));
+  float *P = ptr<float>(c->P);
+  cudaEvent_t a, b;
+  J3G_CUDA(c, cudaEventCreate(&a));
+  J3G_CUDA(c, cudaEventCreate(&b));
+  float best = 0.0f;
+  for (auto &p : cand) {
+    float ms = 0.0f;
+    cudaError_t e = launch_gemm_x3(g, p.second, P, ldp, slice, ptr<int>(c->gerr), c->stream,
+                                   p.first);
+    if (e == cudaSuccess) e = cudaEventRecord(a, c->stream);
+    if (e == cudaSuccess)
+      e = launch_gemm_x3(g, p.second, P, ldp, slice, ptr<int>(c->gerr), c->stream, p.first);
+    if (e == cudaSuccess) e = cudaEventRecord(b, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+    c->launches += 2;
+    if (e != cudaSuccess) {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      return cuda_fail(c, e, "gemm autotune");
+    }
+    if (best == 0.0f || ms < best) {
+      best = ms;
+      plan.tile = p.first;
+      plan.nsplit = p.second;
+      plan.ms = ms;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  c->plans[key] = plan;
+  return J3G_OK;
+}
+
 int batched_forward_impl(j3g_context *c, int nmod, const double *d_models, double *d_data,
                          double *raw_out) {
   const long long K = c->ngrid(), ldK = c->st_ld, R = c->st_rows, np = c->nparm();
@@ -643,16 +740,17 @@ int batched_forward_impl(j3g_context *c, int nmod, const double *d_models, doubl
                                         ptr<double>(c->swork), c->stream));
       c->launches += 2;  // statistics, finalise and split passes
     }
-    const int nsplit = choose_splits(R, (int)(npad / tile), ldK);
-    const int nsp = gemm_splits_used(ldK, nsplit);
     const long long slice = (long long)nmod * R;
-    J3G_TRY(ensure(c, c->P, sizeof(float) * (size_t)nsp * slice));
-    J3G_TRY(ensure(c, c->gerr, sizeof(int)));
     GemmOperands g{c->Jhi.p, c->Jlo.p, R, c->Bhi.p, c->Blo.p, nmod, npad, ldK, true};
+    J3G_TRY(ensure(c, c->gerr, sizeof(int)));
+    j3g_context::GemmPlan plan;
+    J3G_TRY(gemm_plan(c, 0, g, R, slice, plan));
+    c->last_plan[0] = plan;
+    const int nsp = gemm_splits_used(ldK, plan.nsplit);
     {
       TimedScope ts(c, J3G_TIMER_GEMM_FORWARD);
-      J3G_LAUNCH(c, launch_gemm_x3(g, nsplit, ptr<float>(c->P), R, slice, ptr<int>(c->gerr),
-                                   c->stream));
+      J3G_LAUNCH(c, launch_gemm_x3(g, plan.nsplit, ptr<float>(c->P), R, slice,
+                                   ptr<int>(c->gerr), c->stream, plan.tile));
     }
     TimedScope ts(c, J3G_TIMER_REDUCE);
     J3G_LAUNCH(c, launch_splitk_reduce(ptr<float>(c->P), nsp, slice, nmod, (int)R, R,
@@ -714,16 +812,17 @@ int batched_adjoint_impl(j3g_context *c, int nmod, const double *d_models,
                                         nullptr, ptr<double>(c->swork), c->stream));
       c->launches += 2;  // statistics, finalise and split passes
     }
-    const int nsplit = choose_splits(K, (int)(npad / tile), ldR);
-    const int nsp = gemm_splits_used(ldR, nsplit);
     const long long slice = (long long)nmod * K;
-    J3G_TRY(ensure(c, c->P, sizeof(float) * (size_t)nsp * slice));
-    J3G_TRY(ensure(c, c->gerr, sizeof(int)));
     GemmOperands g{c->JThi.p, c->JTlo.p, K, c->Bhi.p, c->Blo.p, nmod, npad, ldR, true};
+    J3G_TRY(ensure(c, c->gerr, sizeof(int)));
+    j3g_context::GemmPlan plan;
+    J3G_TRY(gemm_plan(c, 1, g, K, slice, plan));
+    c->last_plan[1] = plan;
+    const int nsp = gemm_splits_used(ldR, plan.nsplit);
     {
       TimedScope ts(c, J3G_TIMER_GEMM_ADJOINT);
-      J3G_LAUNCH(c, launch_gemm_x3(g, nsplit, ptr<float>(c->P), K, slice, ptr<int>(c->gerr),
-                                   c->stream));
+      J3G_LAUNCH(c, launch_gemm_x3(g, plan.nsplit, ptr<float>(c->P), K, slice,
+                                   ptr<int>(c->gerr), c->stream, plan.tile));
     }
     TimedScope ts(c, J3G_TIMER_REDUCE);
     J3G_LAUNCH(c, launch_splitk_reduce(ptr<float>(c->P), nsp, slice, nmod, (int)K, K, nullptr,
@@ -1141,6 +1240,22 @@ int j3g_get_timing(j3g_context *c, int category, double *total_ms, long long *la
   }
   *total_ms = ms;
   *launches = n;
+  return J3G_OK;
+}
+
+int j3g_set_autotune(j3g_context *c, int enable) {
+  if (!c) return J3G_ERR_ARG;
+  c->autotune = enable != 0;
+  return J3G_OK;
+}
+
+int j3g_get_gemm_plan(const j3g_context *c, int direction, int *nsplit, int *tile,
+                      double *tuned_ms) {
+  if (!c || direction < 0 || direction > 1) return J3G_ERR_ARG;
+  const auto &p = c->last_plan[direction];
+  if (nsplit) *nsplit = p.nsplit;
+  if (tile) *tile = p.tile;
+  if (tuned_ms) *tuned_ms = p.ms;
   return J3G_OK;
 }
 

@@ -820,12 +820,13 @@ int gemm_splits_used(long long ld, int nsplit) {
 }
 
 cudaError_t launch_gemm_x3(const GemmOperands &g, int nsplit, float *P, long long ldp,
-                           long long slice, int *err, cudaStream_t st) {
-  if (g.ld % BK != 0 || g.n_pad % gemm_n_tile((int)g.n) != 0) return cudaErrorInvalidValue;
+                           long long slice, int *err, cudaStream_t st, int tile) {
+  const int nt = tile ? tile : gemm_n_tile((int)g.n);
+  if (nt != 64 && nt != 128 && nt != kPairN) return cudaErrorInvalidValue;
+  if (g.ld % BK != 0 || g.n_pad % nt != 0 || nsplit < 1) return cudaErrorInvalidValue;
   if ((reinterpret_cast<uintptr_t>(g.a_hi) | reinterpret_cast<uintptr_t>(g.a_lo) |
        reinterpret_cast<uintptr_t>(g.b_hi) | reinterpret_cast<uintptr_t>(g.b_lo)) & 15)
     return cudaErrorMisalignedAddress;
-  const int nt = gemm_n_tile((int)g.n);
   if (g.f16) {
     if (nt == kPairN) return launch_pair<true>(g, nsplit, P, ldp, slice, err, st);
     if (nt == 64) return launch_bn<64, true>(g, nsplit, P, ldp, slice, err, st);

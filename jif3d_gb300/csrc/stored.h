@@ -88,7 +88,9 @@ int gemm_splits_used(long long ld, int nsplit);
 // P[split][n][ldp] (split stride `slice`) = per-split sums of
 // Ahi Bhi + Ahi Blo + Alo Bhi; err receives a non-zero code if a bounded
 // wait expired.
+// tile: 0 picks gemm_n_tile(n); 64 or 128 force one-SM tiles of that N, 256
+// the CTA-pair kernel (n_pad must be a multiple of the tile).
 cudaError_t launch_gemm_x3(const GemmOperands &g, int nsplit, float *P, long long ldp,
-                           long long slice, int *err, cudaStream_t st);
+                           long long slice, int *err, cudaStream_t st, int tile = 0);
 
 }  // namespace j3g

@@ -214,3 +214,35 @@ def test_batched_step_captured_in_cuda_graph(ctx, oracle_lib):
         check_groups(s, d_graph[i], oracle_forward(oracle_lib, s, new[i]))
         mis = (d_graph[i] - obs.cpu().numpy()) * w.cpu().numpy()
         assert relerr(g_graph[i], oracle_lqderivative(oracle_lib, s, mis, new[i])) <= TOL
+
+
+def test_autotuned_products(ctx, oracle_lib):
+    """Autotuned tensor-core plans: results within the mixed tolerance, the
+    plan keeps at most 64 k-blocks per split, and the cached plan is reused
+    (same plan, bit-identical results on the second call)."""
+    s = small_survey(W.JOINT, seed=280, nx=16, ny=14, nz=10, nmeas=40)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    ctx.set_autotune(True)
+    try:
+        rng = np.random.default_rng(28)
+        models = s.model[None, :] + 2.0 * rng.normal(size=(300, s.nparm))
+        mis = rng.normal(size=(300, s.stations.shape[0] * 10))
+        d1 = ctx.batched_forward(models)
+        g1 = ctx.batched_lqderivative(models, mis)
+        plans = [ctx.gemm_plan(0), ctx.gemm_plan(1)]
+        d2 = ctx.batched_forward(models)
+        g2 = ctx.batched_lqderivative(models, mis)
+        assert [ctx.gemm_plan(0), ctx.gemm_plan(1)] == plans
+        assert np.array_equal(d1, d2) and np.array_equal(g1, g2)
+    finally:
+        ctx.set_autotune(False)
+    info = ctx.sensitivity_info()
+    kb_fwd = -(-info["cols"] // 64)            # k-blocks of the forward (cells)
+    kb_adj = -(-info["rows"] // 64)            # k-blocks of the adjoint (rows)
+    for p, kb in zip(plans, (kb_fwd, kb_adj)):
+        assert p["tile"] in (128, 256) and p["tuned_ms"] > 0
+        assert p["nsplit"] >= -(-kb // 64)
+    for i in (0, 299):
+        check_groups(s, d1[i], oracle_forward(oracle_lib, s, models[i]))
+        assert relerr(g1[i], oracle_lqderivative(oracle_lib, s, mis[i], models[i])) <= TOL
