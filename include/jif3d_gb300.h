@@ -133,6 +133,24 @@ int j3g_forward_device(j3g_context *ctx, const double *d_model, double *d_data);
 int j3g_lqderivative_device(j3g_context *ctx, const double *d_model, const double *d_misfit,
                             double *d_grad);
 
+/* ---- Station subsets ---------------------------------------------------------
+ * A batch of station subsets of uneven size on the current mesh, model and
+ * kind -- e.g. survey lines or blocks inverted separately -- in one node-term
+ * launch per direction instead of one Calculate / LQDerivative per subset.
+ * Subset k holds the stations h_index[h_offsets[k] .. h_offsets[k+1]) (host
+ * arrays: nsub + 1 non-decreasing offsets from 0, indices into the stations
+ * set with j3g_set_stations; a station may belong to several subsets).
+ * Forward: data of every listed station, subset after subset
+ * (h_offsets[nsub] * data_per_meas values).  Adjoint: d_misfit in the same
+ * layout; one gradient per subset, nsub x nparm values, each
+ * 2 J_k^T (T' misfit_k) over that subset's stations only.  No single reference
+ * counterpart (the reference evaluates each subset with its own calculator). */
+int j3g_subsets_forward_device(j3g_context *ctx, int nsub, const int *h_offsets,
+                               const int *h_index, const double *d_model, double *d_data);
+int j3g_subsets_lqderivative_device(j3g_context *ctx, int nsub, const int *h_offsets,
+                                    const int *h_index, const double *d_model,
+                                    const double *d_misfit, double *d_grads);
+
 /* ---- Device-resident sensitivity matrix ------------------------------------
  * The GPU counterpart of FullSensitivityGravMagCalculator's cached path
  * (GravMag/FullSensitivityGravMagCalculator.h:116-221): J is built once per

@@ -59,6 +59,10 @@ SIGNATURES = {
     "j3g_launch_count": (_I, [_VP, ctypes.POINTER(_LL)]),
     "j3g_set_timing": (_I, [_VP, _I]),
     "j3g_get_timing": (_I, [_VP, _I, _P, ctypes.POINTER(_LL)]),
+    "j3g_subsets_forward_device": (_I, [_VP, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), _VP,
+                                        _VP]),
+    "j3g_subsets_lqderivative_device": (_I, [_VP, _I, ctypes.POINTER(_I), ctypes.POINTER(_I),
+                                             _VP, _VP, _VP]),
     "j3g_set_autotune": (_I, [_VP, _I]),
     "j3g_get_gemm_plan": (_I, [_VP, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), _P]),
     "j3g_probe_fp64": (_I, [_VP, _P]),
@@ -258,6 +262,29 @@ class Context:
         self._check(self._lib.j3g_batched_lqderivative(self._h, m.shape[0], _ptr(m), _ptr(r),
                                                        _ptr(g)))
         return g
+
+    @staticmethod
+    def _subsets(subsets):
+        """Offsets and concatenated indices (int32 host arrays) of station subsets."""
+        off = np.zeros(len(subsets) + 1, dtype=np.int32)
+        off[1:] = np.cumsum([len(x) for x in subsets])
+        idx = (np.concatenate([np.asarray(x, dtype=np.int32) for x in subsets])
+               if off[-1] else np.zeros(1, dtype=np.int32))
+        return off, np.ascontiguousarray(idx, dtype=np.int32)
+
+    def subsets_forward_device(self, subsets, d_model, d_data):
+        off, idx = self._subsets(subsets)
+        ip = ctypes.POINTER(_I)
+        self._check(self._lib.j3g_subsets_forward_device(
+            self._h, len(subsets), off.ctypes.data_as(ip), idx.ctypes.data_as(ip),
+            _VP(d_model), _VP(d_data)))
+
+    def subsets_lqderivative_device(self, subsets, d_model, d_misfit, d_grads):
+        off, idx = self._subsets(subsets)
+        ip = ctypes.POINTER(_I)
+        self._check(self._lib.j3g_subsets_lqderivative_device(
+            self._h, len(subsets), off.ctypes.data_as(ip), idx.ctypes.data_as(ip),
+            _VP(d_model), _VP(d_misfit), _VP(d_grads)))
 
     def set_autotune(self, enable=True):
         self._check(self._lib.j3g_set_autotune(self._h, 1 if enable else 0))

@@ -76,6 +76,15 @@ struct j3g_context {
     float ms = 0.0f;  // timed by the autotuner (0 for the fixed rule)
   };
   bool autotune = false;
+
+  // station subsets (j3g_subsets_*): a context over the concatenated subset
+  // stations, rebuilt when the subsets or this context's setup change
+  long long gen = 0;  // bumped by every set_* call
+  std::vector<double> hsx, hsy, hsz;
+  j3g_context *child = nullptr;
+  std::vector<int> child_off, child_idx;
+  long long child_gen = -1;
+  DevBuf chunks;  // chunk station ranges of a subset adjoint
   std::map<std::array<long long, 4>, GemmPlan> plans;
   GemmPlan last_plan[2];
 
@@ -377,12 +386,19 @@ int forward_device(j3g_context *c, const double *d_model, double *d_data, double
   return J3G_OK;
 }
 
+// Adjoint of all stations into d_grad, or, with sub (nsub + 1 station
+// offsets, sub->back() == nmeas), one gradient per station subset into
+// d_grad + k * nparm; the node path then keeps every chunk of stations
+// inside one subset and sums each subset's chunks on its own.
 int adjoint_device(j3g_context *c, const double *d_model, const double *d_misfit,
-                   double *d_grad) {
+                   double *d_grad, const std::vector<int> *sub = nullptr) {
   J3G_TRY(check_ready(c));
   const long long ngrid = c->ngrid(), nparm = c->nparm();
+  const std::vector<int> all{0, c->nmeas};
+  const std::vector<int> &off = sub ? *sub : all;
+  const int nsub = (int)off.size() - 1;
   if (c->nmeas == 0) {
-    J3G_CUDA(c, cudaMemsetAsync(d_grad, 0, sizeof(double) * (size_t)nparm, c->stream));
+    J3G_CUDA(c, cudaMemsetAsync(d_grad, 0, sizeof(double) * (size_t)nparm * nsub, c->stream));
     return J3G_OK;
   }
   J3G_TRY(ensure_background(c));
@@ -415,36 +431,68 @@ int adjoint_device(j3g_context *c, const double *d_model, const double *d_misfit
     int nchunk = (int)std::max(1LL, std::min(want, maxchunk));
     const int spc = (c->nmeas + nchunk - 1) / nchunk;
     nchunk = (c->nmeas + spc - 1) / spc;
-    J3G_TRY(ensure(c, c->Gpart, sizeof(double) * (size_t)nchunk * nblock * nn));
+    // chunks of at most spc stations that never straddle a subset
+    std::vector<int> starts, first_chunk;
+    const int *d_starts = nullptr;
+    if (sub) {
+      for (int k = 0; k < nsub; ++k) {
+        first_chunk.push_back((int)starts.size());
+        for (int a = off[k]; a < off[k + 1]; a += spc) starts.push_back(a);
+      }
+      first_chunk.push_back((int)starts.size());
+      starts.push_back(c->nmeas);
+      nchunk = (int)starts.size() - 1;
+      J3G_TRY(ensure(c, c->chunks, sizeof(int) * starts.size()));
+      J3G_CUDA(c, cudaMemcpyAsync(c->chunks.p, starts.data(), sizeof(int) * starts.size(),
+                                  cudaMemcpyHostToDevice, c->stream));
+      J3G_CUDA(c, cudaStreamSynchronize(c->stream));  // the host table is a local
+      d_starts = ptr<int>(c->chunks);
+    } else {
+      first_chunk = {0, nchunk};
+    }
+    J3G_TRY(ensure(c, c->Gpart, sizeof(double) * (size_t)std::max(nchunk, 1) * nblock * nn));
     J3G_TRY(ensure(c, c->G, sizeof(double) * (size_t)nblock * nn));
-    {
+    if (nchunk > 0) {
       TimedScope ts(c, J3G_TIMER_NODE_ADJOINT);
-      J3G_LAUNCH(c, launch_node_adjoint(c->kind, m, s, ptr<double>(c->W), spc, nchunk,
+      J3G_LAUNCH(c, launch_node_adjoint(c->kind, m, s, ptr<double>(c->W), spc, nchunk, d_starts,
                                         ptr<double>(c->Gpart), c->stream));
     }
-    J3G_LAUNCH(c, launch_adjoint_combine(m, nchunk, nblock, ptr<double>(c->Gpart),
-                                         ptr<double>(c->G), d_grad, c->stream));
-    c->launches += 2 * nblock - 1;  // chunk sum + cell combine per block
+    for (int k = 0; k < nsub; ++k) {
+      const int c0 = first_chunk[k], nk = first_chunk[k + 1] - c0;
+      J3G_LAUNCH(c, launch_adjoint_combine(m, nk, nblock,
+                                           ptr<double>(c->Gpart) + (size_t)c0 * nblock * nn,
+                                           ptr<double>(c->G), d_grad + (size_t)k * nparm,
+                                           c->stream));
+      c->launches += 2 * nblock - 1;  // chunk sum + cell combine per block
+    }
   } else if (ngrid > 0) {
-    // eight-corner rows, accumulated chunk by chunk
-    J3G_CUDA(c, cudaMemsetAsync(d_grad, 0, sizeof(double) * (size_t)ncolg, c->stream));
+    // eight-corner rows, accumulated chunk by chunk within each subset
     const int chunk = row_chunk(c, ncolg);
     J3G_TRY(ensure(c, c->rows, sizeof(double) * (size_t)chunk * raw * ncolg));
     const MagField mf = mag_field(c);
-    for (int s0 = 0; s0 < c->nmeas; s0 += chunk) {
-      const int ns = std::min(chunk, c->nmeas - s0);
-      J3G_LAUNCH(c, launch_sens_rows(c->kind, false, m, s, s0, ns, mf, nullptr,
-                                   ptr<double>(c->rows), ncolg, c->stream));
-      J3G_LAUNCH(c, launch_rows_tdot(ns * raw, ncolg, ptr<double>(c->rows), ncolg,
-                                   ptr<double>(c->wraw) + (size_t)s0 * raw, d_grad, c->stream));
+    for (int k = 0; k < nsub; ++k) {
+      double *gk = d_grad + (size_t)k * nparm;
+      J3G_CUDA(c, cudaMemsetAsync(gk, 0, sizeof(double) * (size_t)ncolg, c->stream));
+      for (int s0 = off[k]; s0 < off[k + 1]; s0 += chunk) {
+        const int ns = std::min(chunk, off[k + 1] - s0);
+        J3G_LAUNCH(c, launch_sens_rows(c->kind, false, m, s, s0, ns, mf, nullptr,
+                                     ptr<double>(c->rows), ncolg, c->stream));
+        J3G_LAUNCH(c, launch_rows_tdot(ns * raw, ncolg, ptr<double>(c->rows), ncolg,
+                                     ptr<double>(c->wraw) + (size_t)s0 * raw, gk, c->stream));
+      }
+      J3G_LAUNCH(c, launch_scale(ncolg, 2.0, gk, c->stream));
     }
-    J3G_LAUNCH(c, launch_scale(ncolg, 2.0, d_grad, c->stream));
   }
-  if (c->kind == J3G_MAG_GRADIENT && !c->bg.empty())  // background parameters do not respond
-    J3G_CUDA(c, cudaMemsetAsync(d_grad + ngrid, 0, sizeof(double) * c->bg.size(), c->stream));
-  if (nbg > 0)
-    J3G_LAUNCH(c, launch_background_grad(c->kind, c->nmeas, nbg, ptr<double>(c->wraw),
-                                       ptr<double>(c->bgsens), d_grad + ngrid, c->stream));
+  for (int k = 0; k < nsub; ++k) {
+    double *gk = d_grad + (size_t)k * nparm;
+    if (c->kind == J3G_MAG_GRADIENT && !c->bg.empty())  // background parameters do not respond
+      J3G_CUDA(c, cudaMemsetAsync(gk + ngrid, 0, sizeof(double) * c->bg.size(), c->stream));
+    if (nbg > 0)
+      J3G_LAUNCH(c, launch_background_grad(c->kind, off[k + 1] - off[k], nbg,
+                                           ptr<double>(c->wraw) + (size_t)off[k] * raw,
+                                           ptr<double>(c->bgsens) + (size_t)off[k] * raw * nbg,
+                                           gk + ngrid, c->stream));
+  }
   return J3G_OK;
 }
 
@@ -904,13 +952,14 @@ int j3g_destroy(j3g_context *c) {
                     &c->G, &c->F, &c->rows, &c->rowsum, &c->probe, &c->J32, &c->Jhi,
                     &c->Jlo, &c->JThi, &c->JTlo, &c->rowscale, &c->x32, &c->sums, &c->part,
                     &c->Bhi, &c->Blo, &c->P, &c->wst, &c->wrawb, &c->rawb, &c->gerr,
-                    &c->mscale, &c->Jrowsum, &c->mmean, &c->swork};
+                    &c->mscale, &c->Jrowsum, &c->mmean, &c->swork, &c->chunks};
   for (DevBuf *b : bufs)
     if (b->p) cudaFree(b->p);
   for (auto &t : c->timed) {
     cudaEventDestroy(t.second.first);
     cudaEventDestroy(t.second.second);
   }
+  if (c->child) j3g_destroy(c->child);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
   return J3G_OK;
@@ -968,6 +1017,7 @@ int j3g_set_mesh(j3g_context *c, int nx, int ny, int nz, const double *xc, const
   c->mesh_set = true;
   c->bg_dirty = true;
   drop_stored(c);  // the stored sensitivity belongs to the old geometry
+  ++c->gen;
   return J3G_OK;
 }
 
@@ -980,6 +1030,7 @@ int j3g_set_background(j3g_context *c, int nbg, const double *thick) {
   J3G_CUDA(c, cudaStreamSynchronize(c->stream));
   c->bg_dirty = true;
   drop_stored(c);  // the stored sensitivity belongs to the old geometry
+  ++c->gen;
   return J3G_OK;
 }
 
@@ -993,9 +1044,13 @@ int j3g_set_stations(j3g_context *c, int n, const double *x, const double *y, co
   J3G_TRY(upload(c, c->dsz, vz));
   J3G_CUDA(c, cudaStreamSynchronize(c->stream));
   c->nmeas = n;
+  c->hsx.swap(vx);
+  c->hsy.swap(vy);
+  c->hsz.swap(vz);
   c->stations_set = true;
   c->bg_dirty = true;
   drop_stored(c);  // the stored sensitivity belongs to the old geometry
+  ++c->gen;
   return J3G_OK;
 }
 
@@ -1014,6 +1069,7 @@ int j3g_set_kind(j3g_context *c, int kind, double inc, double dec, double fs) {
                      (kind == J3G_MAGNETIC || kind == J3G_MAGNETIZATION));
     if (!ok) c->transform = J3G_T_NONE;
   }
+  ++c->gen;
   return J3G_OK;
 }
 
@@ -1029,6 +1085,7 @@ int j3g_set_transform(j3g_context *c, int transform, double inc, double dec) {
   c->transform = transform;
   c->tinc = inc;
   c->tdec = dec;
+  ++c->gen;
   return J3G_OK;
 }
 
@@ -1054,6 +1111,48 @@ int j3g_lqderivative_device(j3g_context *c, const double *d_model, const double 
   if (!c || !d_model || !d_misfit || !d_grad) return fail(c, J3G_ERR_ARG, "null pointer");
   cudaSetDevice(c->device);
   return adjoint_device(c, d_model, d_misfit, d_grad);
+}
+
+// The context over the concatenated stations of a batch of station subsets
+// (same mesh, background, kind and transform as c, work on c's stream).
+static int subset_child(j3g_context *c, int nsub, const int *off, const int *idx,
+                        j3g_context **out) {
+  J3G_TRY(check_ready(c));
+  if (nsub < 1 || !off || off[0] != 0) return fail(c, J3G_ERR_ARG, "bad subset offsets");
+  for (int k = 0; k < nsub; ++k)
+    if (off[k + 1] < off[k]) return fail(c, J3G_ERR_ARG, "subset offsets must not decrease");
+  const int total = off[nsub];
+  if (total > 0 && !idx) return fail(c, J3G_ERR_ARG, "null subset station index");
+  for (int i = 0; i < total; ++i)
+    if (idx[i] < 0 || idx[i] >= c->nmeas)
+      return fail(c, J3G_ERR_ARG, "subset station index outside the survey");
+  std::vector<int> voff(off, off + nsub + 1), vidx(idx, idx + total);
+  if (!c->child) {
+    int rc = j3g_create(&c->child, c->device);
+    if (rc != J3G_OK) return fail(c, rc, "cannot create the subset context");
+  }
+  j3g_context *ch = c->child;
+  j3g_set_stream(ch, c->stream);
+  if (c->child_gen != c->gen || voff != c->child_off || vidx != c->child_idx) {
+    int rc = j3g_set_mesh(ch, c->nx, c->ny, c->nz, c->X.data(), c->Y.data(), c->Z.data(),
+                          c->xs.data(), c->ys.data(), c->zs.data());
+    if (rc == J3G_OK) rc = j3g_set_background(ch, (int)c->bg.size(), c->bg.data());
+    if (rc == J3G_OK) rc = j3g_set_kind(ch, c->kind, c->inc, c->dec, c->fs);
+    if (rc == J3G_OK) rc = j3g_set_transform(ch, c->transform, c->tinc, c->tdec);
+    std::vector<double> x(total), y(total), z(total);
+    for (int i = 0; i < total; ++i) {
+      x[i] = c->hsx[idx[i]];
+      y[i] = c->hsy[idx[i]];
+      z[i] = c->hsz[idx[i]];
+    }
+    if (rc == J3G_OK) rc = j3g_set_stations(ch, total, x.data(), y.data(), z.data());
+    if (rc != J3G_OK) return fail(c, rc, ch->err);
+    c->child_off.swap(voff);
+    c->child_idx.swap(vidx);
+    c->child_gen = c->gen;
+  }
+  *out = ch;
+  return J3G_OK;
 }
 
 static int host_forward(j3g_context *c, const double *h_model, double *h_data, double *h_sens) {
@@ -1241,6 +1340,32 @@ int j3g_get_timing(j3g_context *c, int category, double *total_ms, long long *la
   *total_ms = ms;
   *launches = n;
   return J3G_OK;
+}
+
+int j3g_subsets_forward_device(j3g_context *c, int nsub, const int *h_offsets,
+                               const int *h_index, const double *d_model, double *d_data) {
+  if (!c || !d_model || !d_data) return fail(c, J3G_ERR_ARG, "null pointer");
+  cudaSetDevice(c->device);
+  j3g_context *ch = nullptr;
+  J3G_TRY(subset_child(c, nsub, h_offsets, h_index, &ch));
+  const long long l0 = ch->launches;
+  const int rc = forward_device(ch, d_model, d_data, nullptr, nullptr);
+  c->launches += ch->launches - l0;
+  return rc == J3G_OK ? J3G_OK : fail(c, rc, ch->err);
+}
+
+int j3g_subsets_lqderivative_device(j3g_context *c, int nsub, const int *h_offsets,
+                                    const int *h_index, const double *d_model,
+                                    const double *d_misfit, double *d_grads) {
+  if (!c || !d_model || !d_misfit || !d_grads) return fail(c, J3G_ERR_ARG, "null pointer");
+  cudaSetDevice(c->device);
+  j3g_context *ch = nullptr;
+  J3G_TRY(subset_child(c, nsub, h_offsets, h_index, &ch));
+  const std::vector<int> off(h_offsets, h_offsets + nsub + 1);
+  const long long l0 = ch->launches;
+  const int rc = adjoint_device(ch, d_model, d_misfit, d_grads, &off);
+  c->launches += ch->launches - l0;
+  return rc == J3G_OK ? J3G_OK : fail(c, rc, ch->err);
 }
 
 int j3g_set_autotune(j3g_context *c, int enable) {

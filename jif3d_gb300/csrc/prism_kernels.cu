@@ -331,7 +331,7 @@ constexpr int kStage = 64;
 template <int KIND>
 __global__ void __launch_bounds__(kThreads)
     k_node_adjoint(MeshView m, StationView st, const double *__restrict__ W, int spc,
-                   double *__restrict__ Gpart) {
+                   const int *__restrict__ chunk_start, double *__restrict__ Gpart) {
   using T = KindTraits<KIND>;
   constexpr int MASK = T::mask;
   constexpr int NCMP = T::ncomp;
@@ -342,8 +342,10 @@ __global__ void __launch_bounds__(kThreads)
   const int nn = (m.nx + 1) * ny1 * nz1;
   const int n = blockIdx.x * kThreads + threadIdx.x;
   const int chunk = blockIdx.y;
-  const int s0 = chunk * spc;
-  const int s1 = min(st.n, s0 + spc);
+  // stations of this chunk: spc apiece, or the ranges of chunk_start (chunks
+  // that never straddle a station subset)
+  const int s0 = chunk_start ? chunk_start[chunk] : chunk * spc;
+  const int s1 = chunk_start ? chunk_start[chunk + 1] : min(st.n, s0 + spc);
   __shared__ double sx[kStage], sy[kStage], sz[kStage], sw[kStage][NCMP];
   int i = 0, j = 0, k = 0;
   if (n < nn) decode_node(n, ny1, nz1, i, j, k);
@@ -720,10 +722,10 @@ cudaError_t launch_comp_weights(int kind, int nmeas, const double *w_raw, const 
 }
 
 cudaError_t launch_node_adjoint(int kind, const MeshView &m, const StationView &s,
-                                const double *W, int spc, int nchunk, double *Gpart,
-                                cudaStream_t st) {
+                                const double *W, int spc, int nchunk, const int *chunk_start,
+                                double *Gpart, cudaStream_t st) {
   dim3 grid(cdiv(m.nnodes(), kThreads), nchunk);
-  J3G_DISPATCH(kind, (k_node_adjoint<K><<<grid, kThreads, 0, st>>>(m, s, W, spc, Gpart)));
+  J3G_DISPATCH(kind, (k_node_adjoint<K><<<grid, kThreads, 0, st>>>(m, s, W, spc, chunk_start, Gpart)));
   return cudaGetLastError();
 }
 

@@ -66,9 +66,11 @@ cudaError_t launch_comp_weights(int kind, int nmeas, const double *w_raw, const 
                                 double *W, cudaStream_t st);
 // Gpart [nchunk][nblock][nnodes] = sum over the chunk's stations of
 // sum_q W_q * F_q, per model block.
+// chunk_start (device, nchunk + 1 values, may be null): explicit station
+// ranges of the chunks instead of stations_per_chunk apiece.
 cudaError_t launch_node_adjoint(int kind, const MeshView &m, const StationView &s,
                                 const double *W, int stations_per_chunk, int nchunk,
-                                double *Gpart, cudaStream_t st);
+                                const int *chunk_start, double *Gpart, cudaStream_t st);
 // grad[b * ngrid + cell] = 2 * sum_corners (-1)^shifts * sum_chunks
 // Gpart[chunk][b][node] for each model block b; G: nblock * nnodes scratch.
 cudaError_t launch_adjoint_combine(const MeshView &m, int nchunk, int nblock, const double *Gpart,
