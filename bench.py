@@ -302,23 +302,33 @@ def run_batched(args, rank, world, local):
     plain_ms = statistics.median(plain_t)
     plain_value = s.ngrid * n / (plain_ms * 1e-3) / 1e6
 
-    # end to end through the C ABI with host buffers
-    models_h = np.ascontiguousarray(s.models)
-    obs_h = d_obs.cpu().numpy()
-    w_h = 1.0 / sig ** 2
+    # end to end through the C ABI with host buffers in pinned memory: every
+    # step copies the models and the misfits in, the data and the gradients
+    # out (the linear adjoint does not read the models); the weighted misfit
+    # is computed on the host between the two calls
+    def pinned(shape):
+        return torch.empty(shape, dtype=torch.float64, pin_memory=True)
+    models_t = pinned(s.models.shape)
+    models_t.copy_(torch.from_numpy(s.models))
+    dh_t, mh_t, gh_t = pinned(data.shape), pinned(data.shape), pinned(s.models.shape)
+    models_h, dh, mh, gh = models_t.numpy(), dh_t.numpy(), mh_t.numpy(), gh_t.numpy()
+    obs_t, w_t = d_obs.cpu(), torch.from_numpy(1.0 / sig ** 2)
+
+    def e2e_step():
+        ctx.batched_forward(models_h, out=dh)
+        torch.mul(torch.sub(dh_t, obs_t, out=mh_t), w_t, out=mh_t)
+        ctx.batched_lqderivative(models_h, mh, out=gh)
+
     for _ in range(2):
-        dh = ctx.batched_forward(models_h)
-        ctx.batched_lqderivative(models_h, (dh - obs_h) * w_h)
+        e2e_step()
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        dh = ctx.batched_forward(models_h)
-        mh = (dh - obs_h) * w_h
-        gh = ctx.batched_lqderivative(models_h, mh)
+        e2e_step()
     t1 = time.perf_counter()
     e2e_s = max_over_ranks(t1 - t0, world)
     e2e = {"value": units * world * args.steps / e2e_s / 1e6, "unit": UNIT,
-           "h2d_bytes_per_step": 8 * (2 * models_h.size + mh.size),
+           "h2d_bytes_per_step": 8 * (models_h.size + mh.size), "host_buffers": "pinned",
            "d2h_bytes_per_step": 8 * (dh.size + gh.size)}
 
     peaks, src = measured_peaks()

@@ -185,8 +185,12 @@ int j3g_stored_lqderivative_device(j3g_context *ctx, const double *d_model,
  * into fp16 hi / lo parts with power-of-two scales, J M ~= Jhi Mhi + Jhi Mlo
  * + Jlo Mhi; the hi*hi products of each 64-wide k-block are drained from TMEM
  * into FP32 register sums, the cross terms accumulate per K split of at most
- * 4096 cells, and the splits are summed in FP64 (about 1e-7 relative error).  The _device forms queue work only; the host forms copy
- * in and out and synchronise. */
+ * 4096 cells, and the splits are summed in FP64 (about 1e-7 relative error).
+ * The _device forms queue work only; the host forms copy in and out and
+ * synchronise (page-locked host buffers copy at full link speed).  The
+ * derivative reads the models only under the FTG-invariant and total-field
+ * transforms, whose derivative depends on the data; otherwise the host form
+ * does not copy them (h_models may then be NULL). */
 int j3g_batched_forward_device(j3g_context *ctx, int nmodels, const double *d_models,
                                double *d_data);
 int j3g_batched_lqderivative_device(j3g_context *ctx, int nmodels, const double *d_models,

@@ -247,19 +247,31 @@ class Context:
                                                               _VP(d_models), _VP(d_misfits),
                                                               _VP(d_grads)))
 
-    def batched_forward(self, models):
+    @staticmethod
+    def _out(out, shape):
+        """A caller's output array (e.g. a view of pinned host memory), checked."""
+        if out is None:
+            return np.zeros(shape)
+        if (out.dtype != np.float64 or not out.flags.c_contiguous or
+                out.size != int(np.prod(shape))):
+            raise J3GError(ERR_ARG, "out must be a C-contiguous float64 array of the result size")
+        return out
+
+    def batched_forward(self, models, out=None):
         s = self.sizes()
         m = _f64(models).reshape(-1, s["nparm"])
-        d = np.zeros((m.shape[0], s["nmeas"] * s["dpm"]))
+        d = self._out(out, (m.shape[0], s["nmeas"] * s["dpm"]))
         self._check(self._lib.j3g_batched_forward(self._h, m.shape[0], _ptr(m), _ptr(d)))
         return d
 
-    def batched_lqderivative(self, models, misfits):
+    def batched_lqderivative(self, models, misfits, out=None):
+        """2 J^T r per model; ``models`` may be None unless the transform is
+        the FTG invariant or the total field (only those read the models)."""
         s = self.sizes()
-        m = _f64(models).reshape(-1, s["nparm"])
-        r = _f64(misfits).reshape(m.shape[0], s["nmeas"] * s["dpm"])
-        g = np.zeros_like(m)
-        self._check(self._lib.j3g_batched_lqderivative(self._h, m.shape[0], _ptr(m), _ptr(r),
+        r = _f64(misfits).reshape(-1, s["nmeas"] * s["dpm"])
+        m = None if models is None else _f64(models).reshape(r.shape[0], s["nparm"])
+        g = self._out(out, (r.shape[0], s["nparm"]))
+        self._check(self._lib.j3g_batched_lqderivative(self._h, r.shape[0], _ptr(m), _ptr(r),
                                                        _ptr(g)))
         return g
 

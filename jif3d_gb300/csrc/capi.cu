@@ -1286,17 +1286,22 @@ int j3g_batched_forward(j3g_context *c, int nmodels, const double *h_models, dou
 
 int j3g_batched_lqderivative(j3g_context *c, int nmodels, const double *h_models,
                              const double *h_misfits, double *h_grads) {
-  if (!c || nmodels < 0 || (nmodels > 0 && (!h_models || !h_misfits || !h_grads)))
+  if (!c || nmodels < 0 || (nmodels > 0 && (!h_misfits || !h_grads)))
     return fail(c, J3G_ERR_ARG, "bad batched arguments");
   cudaSetDevice(c->device);
   J3G_TRY(check_stored(c));
   if (nmodels == 0) return J3G_OK;
+  // only the data-dependent transforms read the models (their forward data)
+  const bool needs_models =
+      c->transform == J3G_T_FTG_INVARIANT || c->transform == J3G_T_TOTAL_FIELD;
+  if (needs_models && !h_models) return fail(c, J3G_ERR_ARG, "this transform needs the models");
   const size_t nm = (size_t)nmodels * c->nparm(), nd = (size_t)nmodels * c->nmeas * c->dpm();
   J3G_TRY(ensure(c, c->model, sizeof(double) * nm));
   J3G_TRY(ensure(c, c->misfit, sizeof(double) * nd));
   J3G_TRY(ensure(c, c->grad, sizeof(double) * nm));
-  J3G_CUDA(c, cudaMemcpyAsync(c->model.p, h_models, sizeof(double) * nm, cudaMemcpyHostToDevice,
-                              c->stream));
+  if (needs_models)
+    J3G_CUDA(c, cudaMemcpyAsync(c->model.p, h_models, sizeof(double) * nm,
+                                cudaMemcpyHostToDevice, c->stream));
   J3G_CUDA(c, cudaMemcpyAsync(c->misfit.p, h_misfits, sizeof(double) * nd,
                               cudaMemcpyHostToDevice, c->stream));
   J3G_TRY(batched_adjoint_impl(c, nmodels, ptr<double>(c->model), ptr<double>(c->misfit),

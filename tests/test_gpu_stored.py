@@ -96,6 +96,41 @@ def test_batched_joint_many_models(ctx, oracle_lib, nmodels):
         assert relerr(g[i], oracle_lqderivative(oracle_lib, s, mis[i], models[i])) <= TOL
 
 
+def test_batched_host_pinned_outputs(ctx):
+    """The host-buffer batched calls write into caller arrays in pinned memory
+    (what an inversion loop reuses each iteration) with the same result as
+    into fresh pageable arrays; a wrong output array is an argument error."""
+    import torch
+    s = small_survey(W.JOINT, seed=260, nx=10, ny=8, nz=6, nmeas=14)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    rng = np.random.default_rng(9)
+    models = s.model[None, :] + rng.normal(size=(4, s.nparm))
+    n = s.stations.shape[0]
+
+    def pinned(shape):
+        return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    mh, dh, rh, gh = pinned(models.shape), pinned((4, n * 10)), pinned((4, n * 10)), \
+        pinned(models.shape)
+    mh[...] = models
+    rh[...] = rng.normal(size=rh.shape)
+    assert ctx.batched_forward(mh, out=dh) is dh
+    assert ctx.batched_lqderivative(mh, rh, out=gh) is gh
+    assert np.array_equal(dh, ctx.batched_forward(models))
+    assert np.array_equal(gh, ctx.batched_lqderivative(models, np.array(rh)))
+    with pytest.raises(capi.J3GError):
+        ctx.batched_forward(mh, out=np.zeros((4, n * 10), dtype=np.float32))
+    with pytest.raises(capi.J3GError):
+        ctx.batched_lqderivative(mh, rh, out=np.zeros((3, s.nparm)))
+    # the linear derivative does not read the models
+    assert np.array_equal(ctx.batched_lqderivative(None, rh), gh)
+    t = small_survey(W.TENSOR, seed=261, transform=W.T_FTG_INVARIANT, nx=6, ny=5, nz=4)
+    W.setup_context(ctx, t)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    with pytest.raises(capi.J3GError):  # the invariant's derivative needs the data
+        ctx.batched_lqderivative(None, np.zeros((2, t.stations.shape[0])))
+
+
 def test_stored_is_dropped_on_new_geometry(ctx):
     s = small_survey(W.SCALAR, seed=5)
     W.setup_context(ctx, s)
