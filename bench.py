@@ -182,6 +182,48 @@ def timed_steps(step, nsteps, stream, flush):
     return times
 
 
+def measure_refinement(s, nmod, steps, stream, flush, local, peaks):
+    """ProjectValues and CombineGradient of the batch between the inversion
+    grid of the workload (coarse) and a forward grid refined 2 x 2 x 2; each
+    pass is timed alone with CUDA events, L2 flushed in between.  Algorithmic
+    bytes: project reads the coarse models and writes the refined ones,
+    combine the reverse (8 bytes a value each way)."""
+    import torch
+    from jif3d_gb300 import capi
+    half = [np.sort(np.concatenate([c, c[:-1] + 0.5 * np.diff(c)]))
+            for c in (s.coords(0), s.coords(1), s.coords(2))]
+    fine = [capi.refine_axis(s.coords(a), (s.xsize, s.ysize, s.zsize)[a], half[a])
+            for a in range(3)]
+    rctx = capi.Context(local)
+    rctx.set_stream(stream.cuda_stream)
+    corner = [np.concatenate([[o], o + np.cumsum(f)[:-1]]) for o, f in zip(s.origin, fine)]
+    rctx.set_mesh(corner[0], corner[1], corner[2], *fine)
+    rctx.set_background(s.bg_thick)
+    rctx.set_refinement(s.xsize, s.ysize, s.zsize)
+    nf = int(np.prod([f.size for f in fine])) + s.bg_thick.size
+    coarse = torch.tensor(s.models, dtype=torch.float64, device=f"cuda:{local}")
+    refined = torch.zeros((nmod, nf), dtype=torch.float64, device=coarse.device)
+    back = torch.zeros_like(coarse)
+    project = lambda: rctx.refine_project_device(nmod, coarse.data_ptr(), refined.data_ptr())
+    combine = lambda: rctx.refine_combine_device(nmod, refined.data_ptr(), back.data_ptr())
+    for _ in range(3):
+        project()
+        combine()
+    torch.cuda.synchronize()
+    t_p = statistics.median(timed_steps(project, steps, stream, flush))
+    t_c = statistics.median(timed_steps(combine, steps, stream, flush))
+    nbytes = 8 * (coarse.numel() + refined.numel())
+    out = {"coarse_cells": s.ngrid, "refined_cells": nf - s.bg_thick.size, "models": nmod,
+           "refined_shape": [f.size for f in fine], "bytes_per_pass": nbytes,
+           "project_ms": t_p, "combine_ms": t_c,
+           "project_gbs": nbytes / (t_p * 1e-3) / 1e9, "combine_gbs": nbytes / (t_c * 1e-3) / 1e9,
+           "hbm_peak_gbs": peaks["hbm_gbs"]}
+    out["project_frac"] = out["project_gbs"] / peaks["hbm_gbs"]
+    out["combine_frac"] = out["combine_gbs"] / peaks["hbm_gbs"]
+    rctx.close()
+    return out
+
+
 def run_batched(args, rank, world, local):
     import torch
     from jif3d_gb300 import capi, workloads as W
@@ -354,6 +396,7 @@ def run_batched(args, rank, world, local):
             "hbm_gbs_of_J_stream": j_bytes / (gemm_ms * 1e-3) / 1e9,
             "hbm_peak_gbs": peaks["hbm_gbs"]}
     ctx.close()
+    refinement = measure_refinement(s, nmod, args.steps, stream, flush, local, peaks)
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -374,6 +417,7 @@ def run_batched(args, rank, world, local):
         "step": "one CUDA graph per step (batched forward, weighted misfit, batched "
                 "adjoint: %d library kernels + 2 torch kernels), replayed" % launches_per_step,
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "clocks": clk,
+        "refinement": refinement,
     }
 
 

@@ -151,6 +151,54 @@ int j3g_subsets_lqderivative_device(j3g_context *ctx, int nsub, const int *h_off
                                     const int *h_index, const double *d_model,
                                     const double *d_misfit, double *d_grads);
 
+/* ---- Model refinement -------------------------------------------------------
+ * An inversion on a coarse grid with the forward calculation on a refined
+ * grid: ModelRefiner (ModelBase/ModelRefiner.h:33-128, ModelRefiner.cpp:17-218)
+ * as ThreeDModelObjective uses it on either side of the forward and the
+ * gradient (Inversion/ThreeDModelObjective.h:188-201, 254-260, 310-324).
+ *
+ * j3g_refine_axis is RefineOneAxis (ModelRefiner.cpp:17-72): the refined cell
+ * sizes of one axis from the coarse corners (ncoarse + 1 values, as
+ * GetXCoordinates returns them), the coarse sizes and nref refinement
+ * coordinates (the fine model's GetXCoordinates; as in the reference the last
+ * one, the end of the domain, is not used).  Every coarse corner is kept, the
+ * refinement coordinates inside each coarse cell are inserted and the last
+ * cell ends where the coarse domain ends.  Writes the count to *nfine and at
+ * most capacity sizes (capacity 0 queries the count).  J3G_ERR_ARG when the
+ * last refined cell would not have a positive size (the reference's
+ * FatalException; *nfine = -1), when nref < 1, or when capacity is too small.
+ * Host only: no context and no GPU needed. */
+int j3g_refine_axis(int ncoarse, const double *h_coarse_coords, const double *h_coarse_sizes,
+                    int nref, const double *h_ref_coords, int capacity, double *h_fine_sizes,
+                    int *nfine);
+/* Attach the coarse (inversion) grid to a context whose mesh is the refined
+ * forward grid.  Along each axis a coarse cell takes refined cells in order
+ * until their summed sizes reach its own size (FindEnd, ModelRefiner.cpp:
+ * 92-102).  Coarse models are [cnx][cny][cnz] cell blocks (three for
+ * magnetisation) followed by the background parameters; j3g_set_mesh clears
+ * the refinement. */
+int j3g_set_refinement(j3g_context *ctx, int cnx, int cny, int cnz, const double *h_xsizes,
+                       const double *h_ysizes, const double *h_zsizes);
+/* Cells and parameters of one coarse model; *covers_all is 0 when some
+ * refined cells lie outside every coarse cell's run (rounding in the walk). */
+int j3g_refinement_info(const j3g_context *ctx, long long *coarse_cells, long long *coarse_nparm,
+                        int *covers_all);
+/* ProjectValues (ModelRefiner.cpp:124-168) for nmodels models: every refined
+ * cell takes the value of its coarse cell; refined cells outside every run
+ * keep their values; the background parameters are copied, as the objective's
+ * ExtraParameterSetter does (ThreeDModelObjective.h:238-248).  Bit-exact. */
+int j3g_refine_project_device(j3g_context *ctx, int nmodels, const double *d_coarse,
+                              double *d_fine);
+/* CombineGradient (ModelRefiner.cpp:170-218): each coarse entry is the sum of
+ * the refined entries of its cell, added in x, y, z order as the reference
+ * adds them (bit-exact); the background entries are copied
+ * (ThreeDModelObjective.h:319-323). */
+int j3g_refine_combine_device(j3g_context *ctx, int nmodels, const double *d_fine,
+                              double *d_coarse);
+/* Host-buffer forms of the two (copy in, run, copy out, synchronise). */
+int j3g_refine_project(j3g_context *ctx, int nmodels, const double *h_coarse, double *h_fine);
+int j3g_refine_combine(j3g_context *ctx, int nmodels, const double *h_fine, double *h_coarse);
+
 /* ---- Device-resident sensitivity matrix ------------------------------------
  * The GPU counterpart of FullSensitivityGravMagCalculator's cached path
  * (GravMag/FullSensitivityGravMagCalculator.h:116-221): J is built once per

@@ -65,6 +65,14 @@ SIGNATURES = {
                                              _VP, _VP, _VP]),
     "j3g_set_autotune": (_I, [_VP, _I]),
     "j3g_get_gemm_plan": (_I, [_VP, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), _P]),
+    "j3g_refine_axis": (_I, [_I, _P, _P, _I, _P, _I, _P, ctypes.POINTER(_I)]),
+    "j3g_set_refinement": (_I, [_VP, _I, _I, _I, _P, _P, _P]),
+    "j3g_refinement_info": (_I, [_VP, ctypes.POINTER(_LL), ctypes.POINTER(_LL),
+                                 ctypes.POINTER(_I)]),
+    "j3g_refine_project_device": (_I, [_VP, _I, _VP, _VP]),
+    "j3g_refine_combine_device": (_I, [_VP, _I, _VP, _VP]),
+    "j3g_refine_project": (_I, [_VP, _I, _P, _P]),
+    "j3g_refine_combine": (_I, [_VP, _I, _P, _P]),
     "j3g_probe_fp64": (_I, [_VP, _P]),
     "j3g_probe_math": (_I, [_I, _I]),
     "j3g_forward_noalloc": (_I, [_I, _I, _I, _I, _VP, _VP, _VP, _I, _VP, _VP, _VP, _D, _D, _D,
@@ -107,6 +115,22 @@ def _ptr(a):
 
 def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def refine_axis(coarse_coords, coarse_sizes, ref_coords):
+    """RefineOneAxis (ModelBase/ModelRefiner.cpp:17-72) on the host: the
+    refined cell sizes of one axis.  ``coarse_coords`` holds the n + 1 corners,
+    ``ref_coords`` the refinement coordinates (the last one is not used).
+    Raises J3GError where the reference throws (a non-positive last cell)."""
+    cc, cs, rc = _f64(coarse_coords), _f64(coarse_sizes), _f64(ref_coords)
+    lib, n = load(), _I()
+    out = np.zeros(cs.size + rc.size)
+    rc_ = lib.j3g_refine_axis(cs.size, _ptr(cc), _ptr(cs), rc.size, _ptr(rc), out.size,
+                              _ptr(out), ctypes.byref(n))
+    if rc_ != OK:
+        raise J3GError(rc_, "Negative cell size in model refinement" if n.value < 0 else
+                       "bad refinement arguments")
+    return out[:n.value].copy()
 
 
 class Context:
@@ -297,6 +321,49 @@ class Context:
         self._check(self._lib.j3g_subsets_lqderivative_device(
             self._h, len(subsets), off.ctypes.data_as(ip), idx.ctypes.data_as(ip),
             _VP(d_model), _VP(d_misfit), _VP(d_grads)))
+
+    # -- model refinement (coarse inversion grid over this context's mesh) --
+    def set_refinement(self, xsizes, ysizes, zsizes):
+        xs, ys, zs = _f64(xsizes), _f64(ysizes), _f64(zsizes)
+        self._check(self._lib.j3g_set_refinement(self._h, xs.size, ys.size, zs.size, _ptr(xs),
+                                                 _ptr(ys), _ptr(zs)))
+
+    def refinement_info(self):
+        cells, nparm, cov = _LL(), _LL(), _I()
+        self._check(self._lib.j3g_refinement_info(self._h, ctypes.byref(cells),
+                                                  ctypes.byref(nparm), ctypes.byref(cov)))
+        return dict(coarse_cells=cells.value, coarse_nparm=nparm.value,
+                    covers_all=bool(cov.value))
+
+    def refine_project_device(self, nmodels, d_coarse, d_fine):
+        self._check(self._lib.j3g_refine_project_device(self._h, int(nmodels), _VP(d_coarse),
+                                                        _VP(d_fine)))
+
+    def refine_combine_device(self, nmodels, d_fine, d_coarse):
+        self._check(self._lib.j3g_refine_combine_device(self._h, int(nmodels), _VP(d_fine),
+                                                        _VP(d_coarse)))
+
+    def refine_project(self, coarse, fine=None):
+        """ProjectValues of one model [coarse nparm] or of a batch [n, coarse
+        nparm]; ``fine`` supplies the values of cells outside every coarse run."""
+        info, s = self.refinement_info(), self.sizes()
+        c = _f64(coarse)
+        n = 1 if c.ndim == 1 else c.shape[0]
+        c = c.reshape(n, info["coarse_nparm"])
+        f = (np.zeros((n, s["nparm"])) if fine is None
+             else np.array(fine, dtype=np.float64).reshape(n, s["nparm"]))
+        self._check(self._lib.j3g_refine_project(self._h, n, _ptr(c), _ptr(f)))
+        return f[0] if np.ndim(coarse) == 1 else f
+
+    def refine_combine(self, fine):
+        """CombineGradient of one gradient [nparm] or of a batch [n, nparm]."""
+        info, s = self.refinement_info(), self.sizes()
+        f = _f64(fine)
+        n = 1 if f.ndim == 1 else f.shape[0]
+        f = f.reshape(n, s["nparm"])
+        c = np.zeros((n, info["coarse_nparm"]))
+        self._check(self._lib.j3g_refine_combine(self._h, n, _ptr(f), _ptr(c)))
+        return c[0] if np.ndim(fine) == 1 else c
 
     def set_autotune(self, enable=True):
         self._check(self._lib.j3g_set_autotune(self._h, 1 if enable else 0))

@@ -20,6 +20,7 @@
 
 #include "../../include/jif3d_gb300.h"
 #include "prism_kernels.h"
+#include "refine.h"
 #include "stored.h"
 
 using namespace j3g;
@@ -87,6 +88,14 @@ struct j3g_context {
   DevBuf chunks;  // chunk station ranges of a subset adjoint
   std::map<std::array<long long, 4>, GemmPlan> plans;
   GemmPlan last_plan[2];
+
+  // model refinement (j3g_set_refinement): the coarse (inversion) grid over
+  // this context's mesh, as the cell walks of the three axes on the device
+  bool refine_set = false;
+  bool refine_covers_all = true;  // every mesh cell belongs to a coarse cell
+  int cn[3] = {0, 0, 0};
+  DevBuf rmaps, rcoarse, rfine;
+  RefineMaps rm{};
 
   // optional per-category kernel timing (j3g_set_timing): event pairs
   // recorded on the context's stream around the dominant launches
@@ -952,7 +961,8 @@ int j3g_destroy(j3g_context *c) {
                     &c->G, &c->F, &c->rows, &c->rowsum, &c->probe, &c->J32, &c->Jhi,
                     &c->Jlo, &c->JThi, &c->JTlo, &c->rowscale, &c->x32, &c->sums, &c->part,
                     &c->Bhi, &c->Blo, &c->P, &c->wst, &c->wrawb, &c->rawb, &c->gerr,
-                    &c->mscale, &c->Jrowsum, &c->mmean, &c->swork, &c->chunks};
+                    &c->mscale, &c->Jrowsum, &c->mmean, &c->swork, &c->chunks, &c->rmaps,
+                    &c->rcoarse, &c->rfine};
   for (DevBuf *b : bufs)
     if (b->p) cudaFree(b->p);
   for (auto &t : c->timed) {
@@ -1015,6 +1025,7 @@ int j3g_set_mesh(j3g_context *c, int nx, int ny, int nz, const double *xc, const
   J3G_TRY(upload(c, c->dzs, c->zs));
   J3G_CUDA(c, cudaStreamSynchronize(c->stream));
   c->mesh_set = true;
+  c->refine_set = false;  // the walks belong to the old mesh
   c->bg_dirty = true;
   drop_stored(c);  // the stored sensitivity belongs to the old geometry
   ++c->gen;
@@ -1400,6 +1411,154 @@ int j3g_synchronize(j3g_context *c) {
   cudaSetDevice(c->device);
   J3G_CUDA(c, cudaStreamSynchronize(c->stream));
   return check_gemm_flag(c);
+}
+
+int j3g_refine_axis(int ncoarse, const double *coarse_coords, const double *coarse_sizes,
+                    int nref, const double *ref_coords, int capacity, double *fine_sizes,
+                    int *nfine) {
+  if (ncoarse < 1 || !coarse_coords || !coarse_sizes || nref < 1 || !ref_coords || !nfine ||
+      capacity < 0 || (capacity > 0 && !fine_sizes))
+    return J3G_ERR_ARG;
+  std::vector<double> f;
+  if (refine_axis(ncoarse, coarse_coords, coarse_sizes, nref, ref_coords, f) != 0) {
+    *nfine = -1;  // non-positive last cell: the reference throws
+    return J3G_ERR_ARG;
+  }
+  *nfine = (int)f.size();
+  if ((int)f.size() > capacity) return J3G_ERR_ARG;
+  std::copy(f.begin(), f.end(), fine_sizes);
+  return J3G_OK;
+}
+
+int j3g_set_refinement(j3g_context *c, int cnx, int cny, int cnz, const double *cxs,
+                       const double *cys, const double *czs) {
+  if (!c) return J3G_ERR_ARG;
+  if (!c->mesh_set || c->ngrid() == 0) return fail(c, J3G_ERR_STATE, "set the forward mesh first");
+  if (cnx < 1 || cny < 1 || cnz < 1 || !cxs || !cys || !czs)
+    return fail(c, J3G_ERR_ARG, "bad coarse grid");
+  if ((long long)cnx * cny * cnz >= (1LL << 30) || c->ngrid() >= (1LL << 30))
+    return fail(c, J3G_ERR_ARG, "grids of 2^30 cells or more are not supported");
+  cudaSetDevice(c->device);
+  const int fn[3] = {c->nx, c->ny, c->nz}, cn[3] = {cnx, cny, cnz};
+  const double *cs[3] = {cxs, cys, czs};
+  const std::vector<double> *fs[3] = {&c->xs, &c->ys, &c->zs};
+  // int layout: owners (fn per axis), begins (cn per axis), ends (cn per axis)
+  std::vector<int> h((size_t)fn[0] + fn[1] + fn[2] + 2 * ((size_t)cnx + cny + cnz));
+  size_t off[3][3], o = 0;
+  for (int a = 0; a < 3; ++a) off[a][0] = o, o += fn[a];
+  for (int a = 0; a < 3; ++a) off[a][1] = o, o += cn[a];
+  for (int a = 0; a < 3; ++a) off[a][2] = o, o += cn[a];
+  bool all = true;
+  for (int a = 0; a < 3; ++a) {
+    int *owner = h.data() + off[a][0];
+    refine_ranges(cn[a], cs[a], fn[a], fs[a]->data(), h.data() + off[a][1], h.data() + off[a][2],
+                  owner);
+    for (int f = 0; f < fn[a]; ++f) all &= owner[f] >= 0;
+  }
+  J3G_TRY(ensure(c, c->rmaps, h.size() * sizeof(int)));
+  J3G_CUDA(c, cudaMemcpyAsync(c->rmaps.p, h.data(), h.size() * sizeof(int),
+                              cudaMemcpyHostToDevice, c->stream));
+  J3G_CUDA(c, cudaStreamSynchronize(c->stream));
+  const int *d = ptr<int>(c->rmaps);
+  for (int a = 0; a < 3; ++a) {
+    c->rm.owner[a] = d + off[a][0];
+    c->rm.begin[a] = d + off[a][1];
+    c->rm.end[a] = d + off[a][2];
+    c->rm.cn[a] = cn[a];
+    c->rm.fn[a] = fn[a];
+    c->cn[a] = cn[a];
+  }
+  c->refine_covers_all = all;
+  c->refine_set = true;
+  return J3G_OK;
+}
+
+namespace {
+// cell blocks and extra parameters of a model vector of this context's kind
+void refine_layout(const j3g_context *c, int &nblock, int &nextra) {
+  nblock = c->kind == J3G_MAGNETIZATION ? 3 : 1;
+  nextra = c->kind == J3G_MAGNETIZATION ? 0 : (int)c->bg.size();
+}
+long long coarse_nparm(const j3g_context *c) {
+  int nblock, nextra;
+  refine_layout(c, nblock, nextra);
+  return (long long)nblock * c->cn[0] * c->cn[1] * c->cn[2] + nextra;
+}
+}  // namespace
+
+int j3g_refinement_info(const j3g_context *c, long long *coarse_cells, long long *coarse_nparm_out,
+                        int *covers_all) {
+  if (!c) return J3G_ERR_ARG;
+  if (!c->refine_set) return J3G_ERR_STATE;
+  if (coarse_cells) *coarse_cells = (long long)c->cn[0] * c->cn[1] * c->cn[2];
+  if (coarse_nparm_out) *coarse_nparm_out = coarse_nparm(c);
+  if (covers_all) *covers_all = c->refine_covers_all ? 1 : 0;
+  return J3G_OK;
+}
+
+int j3g_refine_project_device(j3g_context *c, int nmodels, const double *d_coarse,
+                              double *d_fine) {
+  if (!c || nmodels < 0 || (nmodels > 0 && (!d_coarse || !d_fine)))
+    return fail(c, J3G_ERR_ARG, "bad refinement arguments");
+  if (!c->refine_set) return fail(c, J3G_ERR_STATE, "no refinement set for this mesh");
+  cudaSetDevice(c->device);
+  int nblock, nextra;
+  refine_layout(c, nblock, nextra);
+  J3G_LAUNCH(c, launch_refine_project(c->rm, nmodels, nblock, nextra, d_coarse, d_fine,
+                                      c->stream));
+  return J3G_OK;
+}
+
+int j3g_refine_combine_device(j3g_context *c, int nmodels, const double *d_fine,
+                              double *d_coarse) {
+  if (!c || nmodels < 0 || (nmodels > 0 && (!d_coarse || !d_fine)))
+    return fail(c, J3G_ERR_ARG, "bad refinement arguments");
+  if (!c->refine_set) return fail(c, J3G_ERR_STATE, "no refinement set for this mesh");
+  cudaSetDevice(c->device);
+  int nblock, nextra;
+  refine_layout(c, nblock, nextra);
+  J3G_LAUNCH(c, launch_refine_combine(c->rm, nmodels, nblock, nextra, d_fine, d_coarse,
+                                      c->stream));
+  return J3G_OK;
+}
+
+int j3g_refine_project(j3g_context *c, int nmodels, const double *h_coarse, double *h_fine) {
+  if (!c || nmodels < 0 || (nmodels > 0 && (!h_coarse || !h_fine)))
+    return fail(c, J3G_ERR_ARG, "bad refinement arguments");
+  if (!c->refine_set) return fail(c, J3G_ERR_STATE, "no refinement set for this mesh");
+  if (nmodels == 0) return J3G_OK;
+  cudaSetDevice(c->device);
+  const size_t nc = (size_t)nmodels * coarse_nparm(c), nf = (size_t)nmodels * c->nparm();
+  J3G_TRY(ensure(c, c->rcoarse, nc * sizeof(double)));
+  J3G_TRY(ensure(c, c->rfine, nf * sizeof(double)));
+  J3G_CUDA(c, cudaMemcpyAsync(c->rcoarse.p, h_coarse, nc * sizeof(double),
+                              cudaMemcpyHostToDevice, c->stream));
+  if (!c->refine_covers_all)  // uncovered cells keep the caller's values
+    J3G_CUDA(c, cudaMemcpyAsync(c->rfine.p, h_fine, nf * sizeof(double), cudaMemcpyHostToDevice,
+                                c->stream));
+  J3G_TRY(j3g_refine_project_device(c, nmodels, ptr<double>(c->rcoarse), ptr<double>(c->rfine)));
+  J3G_CUDA(c, cudaMemcpyAsync(h_fine, c->rfine.p, nf * sizeof(double), cudaMemcpyDeviceToHost,
+                              c->stream));
+  J3G_CUDA(c, cudaStreamSynchronize(c->stream));
+  return J3G_OK;
+}
+
+int j3g_refine_combine(j3g_context *c, int nmodels, const double *h_fine, double *h_coarse) {
+  if (!c || nmodels < 0 || (nmodels > 0 && (!h_coarse || !h_fine)))
+    return fail(c, J3G_ERR_ARG, "bad refinement arguments");
+  if (!c->refine_set) return fail(c, J3G_ERR_STATE, "no refinement set for this mesh");
+  if (nmodels == 0) return J3G_OK;
+  cudaSetDevice(c->device);
+  const size_t nc = (size_t)nmodels * coarse_nparm(c), nf = (size_t)nmodels * c->nparm();
+  J3G_TRY(ensure(c, c->rcoarse, nc * sizeof(double)));
+  J3G_TRY(ensure(c, c->rfine, nf * sizeof(double)));
+  J3G_CUDA(c, cudaMemcpyAsync(c->rfine.p, h_fine, nf * sizeof(double), cudaMemcpyHostToDevice,
+                              c->stream));
+  J3G_TRY(j3g_refine_combine_device(c, nmodels, ptr<double>(c->rfine), ptr<double>(c->rcoarse)));
+  J3G_CUDA(c, cudaMemcpyAsync(h_coarse, c->rcoarse.p, nc * sizeof(double),
+                              cudaMemcpyDeviceToHost, c->stream));
+  J3G_CUDA(c, cudaStreamSynchronize(c->stream));
+  return J3G_OK;
 }
 
 int j3g_probe_fp64(j3g_context *c, double *gflops) {

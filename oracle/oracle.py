@@ -36,7 +36,10 @@ _ref = None
 def build(force: bool = False) -> None:
     """Compile liboracle.so (and the reference box-term library when the
     jif3D sources exist on this machine)."""
-    if force or not os.path.exists(LIB_PATH):
+    srcs = [os.path.join(HERE, f) for f in ("prism_oracle.c", "refine_oracle.c")]
+    stale = not os.path.exists(LIB_PATH) or any(
+        os.path.getmtime(f) > os.path.getmtime(LIB_PATH) for f in srcs)
+    if force or stale:
         subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
     ref_src = os.environ.get("JIF3D_REF", "/root/reference/jif3D")
     if os.path.isdir(ref_src) and (force or not os.path.exists(REF_PATH)):
@@ -46,8 +49,7 @@ def build(force: bool = False) -> None:
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
-            build()
+        build()
         _lib = ctypes.CDLL(LIB_PATH)
         box_args = [_D] * 9
         for name in ("orc_grav_box", "orc_uxx_box", "orc_uxy_box"):
@@ -68,6 +70,11 @@ def lib():
         _lib.orc_lqderivative.restype = _I
         _lib.orc_sens_matvec.argtypes = [_I, _I, _P, _P, _P]
         _lib.orc_sens_rmatvec2.argtypes = [_I, _I, _P, _P, _P]
+        _lib.orc_refine_axis.argtypes = [_I, _P, _P, _I, _P, _P]
+        _lib.orc_refine_axis.restype = _I
+        walk = [_I, _I, _I, _P, _P, _P, _I, _I, _I, _P, _P, _P, _P, _P]
+        _lib.orc_refine_project.argtypes = walk
+        _lib.orc_refine_combine.argtypes = walk
     return _lib
 
 
@@ -192,3 +199,48 @@ def sens_rmatvec2(J, r):
     g = np.zeros(J.shape[1])
     lib().orc_sens_rmatvec2(J.shape[0], J.shape[1], _ptr(J), _ptr(r), _ptr(g))
     return g
+
+
+# -- model refinement (ModelBase/ModelRefiner.cpp) ----------------------------
+def corners(origin, sizes):
+    """ThreeDModelBase::CalcCoords (ModelBase/ThreeDModelBase.cpp:96-113)."""
+    c = np.empty(len(sizes) + 1)
+    c[0] = s = float(origin)
+    for i, v in enumerate(sizes):
+        s = s + float(v)
+        c[i + 1] = s
+    return c
+
+
+def refine_axis(old_coords, old_sizes, ref_coords):
+    """RefineOneAxis: refined sizes, or None where the reference throws."""
+    oc, os_, rc = _f64(old_coords), _f64(old_sizes), _f64(ref_coords)
+    out = np.zeros(os_.size + rc.size)
+    n = lib().orc_refine_axis(os_.size, _ptr(oc), _ptr(os_), rc.size, _ptr(rc), _ptr(out))
+    return None if n < 0 else out[:n].copy()
+
+
+def _walk_args(csizes, fsizes):
+    cs = [_f64(v) for v in csizes]
+    fs = [_f64(v) for v in fsizes]
+    return cs, fs, [c.size for c in cs] + [_ptr(c) for c in cs] + \
+        [f.size for f in fs] + [_ptr(f) for f in fs]
+
+
+def refine_project(csizes, fsizes, coarse, fine=None):
+    """ProjectValues of one cell block; ``fine`` (if given) supplies the values
+    of refined cells outside every coarse run."""
+    cs, fs, args = _walk_args(csizes, fsizes)
+    out = np.zeros(int(np.prod([f.size for f in fs]))) if fine is None else _f64(fine).copy()
+    c = _f64(coarse)
+    lib().orc_refine_project(*args, _ptr(c), _ptr(out))
+    return out
+
+
+def refine_combine(csizes, fsizes, fine):
+    """CombineGradient of one cell block."""
+    cs, fs, args = _walk_args(csizes, fsizes)
+    out = np.zeros(int(np.prod([c.size for c in cs])))
+    f = _f64(fine)
+    lib().orc_refine_combine(*args, _ptr(f), _ptr(out))
+    return out

@@ -355,3 +355,99 @@ def test_lqderivative_equals_2JTr_magnetic_kinds(oracle_lib):
         _, J = p.forward(s.model, True)
         ref = O.sens_rmatvec2(J, r)
         np.testing.assert_allclose(g, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
+
+
+# -- model refinement (ModelBase/test_ModelRefiner.cpp) -------------------------
+def refiner_case():
+    """MakeModelandRefinement (test_ModelRefiner.cpp:37-75): a 2 x 3 x 5 coarse
+    grid of 50 / 40 / 30 m cells, refinement coordinates 10 i, 20 i, 5 i."""
+    cs = [np.full(2, 50.0), np.full(3, 40.0), np.full(5, 30.0)]
+    refs = [10.0 * np.arange(20), 20.0 * np.arange(20), 5.0 * np.arange(50)]
+    return cs, refs
+
+
+def test_refiner_basic_axis_refinement(oracle_lib):
+    """basic_axis_refinement (test_ModelRefiner.cpp:77-113): the refined
+    corners are the union of coarse and refinement coordinates, the domain
+    ends where the coarse one ends."""
+    O = oracle_lib
+    cs, refs = refiner_case()
+    for c, r in zip(cs, refs):
+        cc = O.corners(0.0, c)
+        f = O.refine_axis(cc, c, r)
+        fc = O.corners(0.0, f)
+        union = np.unique(np.concatenate([r, cc]))
+        assert np.array_equal(fc[:-1], union[:f.size])      # CheckAxis :20-35
+        assert fc[-1] == cc[-1]                             # :99-110
+    # the reference's sizes: 10 x 10 m, 6 x 20 m, 30 x 5 m
+    assert [O.refine_axis(O.corners(0.0, c), c, r).size for c, r in zip(cs, refs)] == [10, 6, 30]
+
+
+def test_refiner_model_projection(oracle_lib):
+    """model_projection (test_ModelRefiner.cpp:115-147): a unit fine gradient
+    combines to 60 on every coarse cell (5 x 2 x 6 refined cells each), and
+    every refined cell takes the value of the coarse cell that contains it."""
+    O = oracle_lib
+    cs, refs = refiner_case()
+    fs = [O.refine_axis(O.corners(0.0, c), c, r) for c, r in zip(cs, refs)]
+    nfine = int(np.prod([f.size for f in fs]))
+    g = O.refine_combine(cs, fs, np.ones(nfine))
+    assert g.size == 30 and np.all(g == 60.0)
+    coarse = np.arange(30, dtype=float)                     # std::iota (:128-130)
+    fine = O.refine_project(cs, fs, coarse).reshape([f.size for f in fs])
+    cen = [O.corners(0.0, f)[:-1] + 0.5 * f for f in fs]
+    owner = [np.searchsorted(O.corners(0.0, c), x) - 1 for c, x in zip(cs, cen)]
+    expect = coarse.reshape(2, 3, 5)[np.ix_(*owner)]
+    assert np.array_equal(fine, expect)
+
+
+def test_refiner_walk_edge_cases(oracle_lib):
+    """Refined cells past every coarse run keep their values; coarse corners
+    that repeat refinement coordinates are not doubled; a coarse cell whose
+    walk finds no refined cells combines to 0."""
+    O = oracle_lib
+    cs = [np.array([10.0]), np.array([4.0, 6.0]), np.array([5.0])]
+    fs = [np.array([5.0, 5.0, 5.0]), np.array([2.0, 2.0, 6.0]), np.array([5.0])]
+    fine0 = np.full(9, -7.0)
+    fine = O.refine_project(cs, fs, np.array([1.0, 2.0]), fine0).reshape(3, 3, 1)
+    assert np.all(fine[:2, :2] == 1.0) and np.all(fine[:2, 2] == 2.0)
+    assert np.all(fine[2] == -7.0)
+    assert np.array_equal(O.refine_combine(cs, fs, np.arange(9.0)), [0 + 1 + 3 + 4, 2 + 5])
+    # refinement coordinates equal to coarse corners
+    f = O.refine_axis([0.0, 10.0, 20.0], [10.0, 10.0], [0.0, 5.0, 10.0, 15.0, 20.0])
+    assert np.array_equal(f, [5.0, 5.0, 5.0, 5.0])
+    cs2 = [np.array([10.0]), np.array([1.0]), np.array([3.0, 3.0])]
+    fs2 = [np.array([10.0]), np.array([1.0]), np.array([3.0, 3.0, 1.0])]
+    assert np.array_equal(O.refine_combine(cs2, fs2, np.array([1.0, 2.0, 4.0])), [1.0, 2.0])
+    cs3 = [np.array([1.0]), np.array([1.0]), np.array([3.0, 3.0, 2.0])]
+    fs3 = [np.array([1.0]), np.array([1.0]), np.array([4.0, 4.0])]
+    assert np.array_equal(O.refine_combine(cs3, fs3, np.array([1.0, 2.0])), [1.0, 2.0, 0.0])
+
+
+def test_capi_refine_axis_matches_oracle(oracle_lib):
+    """j3g_refine_axis (host code of the library) against the oracle on
+    irregular axes with rounding in the corner sums (bit-exact)."""
+    from jif3d_gb300 import capi
+    O = oracle_lib
+    rng = np.random.default_rng(77)
+    for t in range(200):
+        n = int(rng.integers(1, 9))
+        c = rng.uniform(0.05, 3.0, n).round(int(rng.integers(1, 4)))
+        cc = O.corners(round(float(rng.uniform(-5, 5)), 2), c)
+        r = np.sort(rng.uniform(cc[0] - 1, cc[-1] + 1, int(rng.integers(1, 30))).round(2))
+        if t % 3 == 0:
+            r = np.unique(np.concatenate([r, cc[rng.integers(0, n, 2)]]))
+        ref = O.refine_axis(cc, c, r)
+        if ref is None:
+            with pytest.raises(capi.J3GError):
+                capi.refine_axis(cc, c, r)
+            continue
+        got = capi.refine_axis(cc, c, r)
+        assert np.array_equal(got, ref), (cc, c, r)
+    with pytest.raises(capi.J3GError):
+        capi.refine_axis([0.0, 1.0], [1.0], [])
+    # a last coarse cell of zero size leaves a last refined cell of zero size:
+    # the reference throws (ModelRefiner.cpp:63-71)
+    assert O.refine_axis([0.0, 10.0, 10.0], [10.0, 0.0], [0.0, 5.0, 10.0]) is None
+    with pytest.raises(capi.J3GError):
+        capi.refine_axis([0.0, 10.0, 10.0], [10.0, 0.0], [0.0, 5.0, 10.0])
