@@ -9,6 +9,7 @@
 // cross to the host (sensitivity rows only when asked for).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1468,6 +1469,9 @@ int j3g_set_refinement(j3g_context *c, int cnx, int cny, int cnz, const double *
     c->rm.fn[a] = fn[a];
     c->cn[a] = cn[a];
   }
+  c->rm.zrun_max = 0;
+  for (int k = 0; k < cnz; ++k)
+    c->rm.zrun_max = std::max(c->rm.zrun_max, h[off[2][2] + k] - h[off[2][1] + k]);
   c->refine_covers_all = all;
   c->refine_set = true;
   return J3G_OK;

@@ -31,6 +31,7 @@ struct RefineMaps {
   const int *end[3];
   int cn[3];            // coarse cells per axis
   int fn[3];            // refined cells per axis
+  int zrun_max;         // longest z run of refined cells of one coarse cell
 };
 
 // ProjectValues (:124-168) for nmodels models of nblock cell blocks followed

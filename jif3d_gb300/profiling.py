@@ -5,6 +5,7 @@
     python -m jif3d_gb300.profiling gemm [--stations 128]  # tensor-core batched products
     python -m jif3d_gb300.profiling stream [--stations 400] # FP32 streaming products
     python -m jif3d_gb300.profiling batched [--steps 2]     # full config-4 batched steps
+    python -m jif3d_gb300.profiling refine [--models 32]    # model refinement passes
 
 Each case runs a few launches on a few-MB problem so that an ncu capture of
 it ends by itself; ``batched`` runs the full 256-model config-4 step (7.5 GB of
@@ -94,6 +95,31 @@ def case_batched(steps: int) -> None:
     ctx.close()
 
 
+def case_refine(models: int) -> None:
+    """Projection and combination between the config-4 grid (coarse) and a
+    grid refined 2 x 2 x 2 (128 x 128 x 64), for ``models`` models: one launch
+    of each (32 models: 268 MB of refined values, larger than L2)."""
+    import torch
+    from . import capi, workloads as W
+    s = W.config4(nmodels=models)
+    half = [np.sort(np.concatenate([c, c[:-1] + 0.5 * np.diff(c)]))
+            for c in (s.coords(0), s.coords(1), s.coords(2))]
+    fine = [capi.refine_axis(s.coords(a), (s.xsize, s.ysize, s.zsize)[a], half[a])
+            for a in range(3)]
+    ctx = capi.Context(0)
+    corner = [np.concatenate([[o], o + np.cumsum(f)[:-1]]) for o, f in zip(s.origin, fine)]
+    ctx.set_mesh(corner[0], corner[1], corner[2], *fine)
+    ctx.set_refinement(s.xsize, s.ysize, s.zsize)
+    coarse = torch.tensor(s.models, dtype=torch.float64, device="cuda")
+    refined = torch.zeros((models, ctx.sizes()["nparm"]), dtype=torch.float64, device="cuda")
+    back = torch.zeros_like(coarse)
+    ctx.refine_project_device(models, coarse.data_ptr(), refined.data_ptr())
+    ctx.refine_combine_device(models, refined.data_ptr(), back.data_ptr())
+    ctx.synchronize()
+    print("refine case ok", [f.size for f in fine], models, "models", float(back[0, 0]))
+    ctx.close()
+
+
 def case_fp64_weights(n_iter: int) -> None:
     from . import capi
     lib = capi.load()
@@ -117,6 +143,8 @@ def main(argv=None) -> None:
     st.add_argument("--stations", type=int, default=400)
     b = sub.add_parser("batched")
     b.add_argument("--steps", type=int, default=2)
+    r = sub.add_parser("refine")
+    r.add_argument("--models", type=int, default=32)
     a = p.parse_args(argv)
     if a.case == "node":
         case_node(a.stations)
@@ -126,6 +154,8 @@ def main(argv=None) -> None:
         case_stream(a.stations)
     elif a.case == "batched":
         case_batched(a.steps)
+    elif a.case == "refine":
+        case_refine(a.models)
     elif a.case == "fp64-weights":
         case_fp64_weights(a.iters)
 

@@ -3,7 +3,7 @@ coarse-grid objective built on it (Inversion/ThreeDModelObjective.h:254-260,
 310-324) against the oracle.
 
 Tolerances: projection and combination are copies and ordered FP64 sums, so
-they must agree bit for bit (np.array_equal); the forward and gradient on the
+they must agree bit for bit (signed zeros included); the forward and gradient on the
 refined grid are the FP64 path (relative norm error <= 1e-10).
 """
 import dataclasses
@@ -16,6 +16,12 @@ from jif3d_gb300 import capi, workloads as W
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-10
+
+
+def same_bits(a, b):
+    """Bit-for-bit equality (np.array_equal does not tell -0.0 from +0.0)."""
+    a, b = np.ascontiguousarray(a, dtype=np.float64), np.ascontiguousarray(b, dtype=np.float64)
+    return a.shape == b.shape and np.array_equal(a.view(np.int64), b.view(np.int64))
 
 
 def refine(s, refs):
@@ -78,7 +84,7 @@ def test_reference_refiner_case_on_device(ctx, oracle_lib):
     info = ctx.refinement_info()
     assert info == dict(coarse_cells=30, coarse_nparm=30, covers_all=True)
     fine = ctx.refine_project(s.model)
-    assert np.array_equal(fine, oracle_project(oracle_lib, s, f, s.model, 1, 0))
+    assert same_bits(fine, oracle_project(oracle_lib, s, f, s.model, 1, 0))
     assert np.all(ctx.refine_combine(np.ones(f.ngrid)) == 60.0)
 
 
@@ -105,16 +111,16 @@ def test_project_combine_bit_exact(ctx, oracle_lib, kind, nmodels):
                      for i in range(nmodels)])
     refC = np.stack([oracle_combine(oracle_lib, s, f, Fg[i], nblock, nextra)
                      for i in range(nmodels)])
-    assert np.array_equal(ctx.refine_project(C), refF)
-    assert np.array_equal(ctx.refine_combine(Fg), refC)
+    assert same_bits(ctx.refine_project(C), refF)
+    assert same_bits(ctx.refine_combine(Fg), refC)
     dC, dF = torch.tensor(C, device="cuda"), torch.zeros(refF.shape, dtype=torch.float64,
                                                          device="cuda")
     ctx.refine_project_device(nmodels, dC.data_ptr(), dF.data_ptr())
     dG, dOut = torch.tensor(Fg, device="cuda"), torch.zeros_like(dC)
     ctx.refine_combine_device(nmodels, dG.data_ptr(), dOut.data_ptr())
     ctx.synchronize()
-    assert np.array_equal(dF.cpu().numpy(), refF)
-    assert np.array_equal(dOut.cpu().numpy(), refC)
+    assert same_bits(dF.cpu().numpy(), refF)
+    assert same_bits(dOut.cpu().numpy(), refC)
 
 
 def test_uncovered_cells_keep_values(ctx, oracle_lib):
@@ -131,14 +137,14 @@ def test_uncovered_cells_keep_values(ctx, oracle_lib):
     assert not ctx.refinement_info()["covers_all"]
     prev = np.full(9, -7.0)
     ref = oracle_project(oracle_lib, s, f, s.model, 1, 0, prev)
-    assert np.array_equal(ctx.refine_project(s.model, prev), ref)
+    assert same_bits(ctx.refine_project(s.model, prev), ref)
     dF = torch.full((9,), -7.0, dtype=torch.float64, device="cuda")
     dC = torch.tensor(s.model, device="cuda")
     ctx.refine_project_device(1, dC.data_ptr(), dF.data_ptr())
     ctx.synchronize()
-    assert np.array_equal(dF.cpu().numpy(), ref)
+    assert same_bits(dF.cpu().numpy(), ref)
     g = np.arange(9.0)
-    assert np.array_equal(ctx.refine_combine(g), oracle_combine(oracle_lib, s, f, g, 1, 0))
+    assert same_bits(ctx.refine_combine(g), oracle_combine(oracle_lib, s, f, g, 1, 0))
 
 
 @pytest.mark.parametrize("kind", [W.SCALAR, W.TENSOR, W.MAGNETIC])
@@ -186,8 +192,8 @@ def test_refinement_state_and_errors(ctx):
     ctx.set_refinement(*coarse_sizes(s))
     assert ctx.refinement_info()["coarse_nparm"] == s.nparm
     # the identity refinement: projection and combination are copies
-    assert np.array_equal(ctx.refine_project(s.model), s.model)
-    assert np.array_equal(ctx.refine_combine(s.model), s.model)
+    assert same_bits(ctx.refine_project(s.model), s.model)
+    assert same_bits(ctx.refine_combine(s.model), s.model)
     W.setup_context(ctx, s)
     with pytest.raises(capi.J3GError):
         ctx.refinement_info()
@@ -220,8 +226,46 @@ def test_large_refinement_adjoint_identity(ctx, oracle_lib):
     ctx.refine_combine_device(2, dG.data_ptr(), dOut.data_ptr())
     ctx.synchronize()
     PF, PtG = dF.cpu().numpy(), dOut.cpu().numpy()
-    assert np.array_equal(PF[1], oracle_project(oracle_lib, s, f, C[1], 1, 0))
-    assert np.array_equal(PtG[0], oracle_combine(oracle_lib, s, f, Fg[0], 1, 0))
+    assert same_bits(PF[1], oracle_project(oracle_lib, s, f, C[1], 1, 0))
+    assert same_bits(PtG[0], oracle_combine(oracle_lib, s, f, Fg[0], 1, 0))
     for i in range(2):
         lhs, rhs = float(PF[i] @ Fg[i]), float(C[i] @ PtG[i])
         assert abs(lhs - rhs) <= 1e-12 * np.linalg.norm(PF[i]) * np.linalg.norm(Fg[i])
+
+
+@pytest.mark.parametrize("case", ["long_rows", "odd_rows", "long_runs"])
+def test_kernel_paths(ctx, oracle_lib, case):
+    """The kernels' launch variants against the oracle, bit for bit: rows of
+    more than 64 refined z cells and more than 32 coarse z cells (lanes loop
+    over chunks), odd row lengths (no paired stores), z runs longer than 4
+    (the run-length loop)."""
+    import torch
+    zs = {"long_rows": np.full(40, 8.0), "odd_rows": np.array([5.0, 7.0, 9.0]),
+          "long_runs": np.array([12.0, 20.0])}[case]
+    s = small_survey(W.SCALAR, seed=60, nx=3, ny=2, nz=zs.size, bg=False,
+                     origin=(0.0, 0.0, 0.0))
+    s = dataclasses.replace(s, zsize=zs, model=np.zeros(3 * 2 * zs.size))
+    zc = s.coords(2)
+    zref = {"long_rows": np.sort(np.concatenate([zc, zc[:-1] + 4.0])),
+            "odd_rows": np.array([0.0, 2.0, 5.0, 7.0, 9.0, 12.0, 15.0, 21.0]),
+            "long_runs": np.arange(0.0, 33.0, 2.0)}[case]
+    f = refine(s, [s.coords(0), s.coords(1), zref])
+    expect_fnz = {"long_rows": 80, "odd_rows": 7, "long_runs": 16}[case]
+    assert f.zsize.size == expect_fnz
+    fine_setup(ctx, s, f)
+    rng = np.random.default_rng(61)
+    C = rng.normal(size=(2, s.ngrid))
+    Fg = rng.normal(size=(2, f.ngrid))
+    # signed zeros: a sum that starts with -0.0 (or holds only zeros) must
+    # come out as the reference's 0.0 + ... does
+    Fg[:, ::7] = -0.0
+    Fg[1, : 2 * f.zsize.size] = -0.0
+    dC, dF = torch.tensor(C, device="cuda"), torch.zeros((2, f.ngrid), dtype=torch.float64,
+                                                         device="cuda")
+    dG, dOut = torch.tensor(Fg, device="cuda"), torch.zeros_like(dC)
+    ctx.refine_project_device(2, dC.data_ptr(), dF.data_ptr())
+    ctx.refine_combine_device(2, dG.data_ptr(), dOut.data_ptr())
+    ctx.synchronize()
+    for i in range(2):
+        assert same_bits(dF[i].cpu().numpy(), oracle_project(oracle_lib, s, f, C[i], 1, 0))
+        assert same_bits(dOut[i].cpu().numpy(), oracle_combine(oracle_lib, s, f, Fg[i], 1, 0))
