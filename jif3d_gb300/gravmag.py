@@ -192,10 +192,30 @@ class ThreeDMagnetizationModel(ThreeDModelBase):
 
 
 class GeneralData:
-    """Measurement positions (DataBase/GeneralData.h)."""
+    """Measurement positions, data and errors (DataBase/GeneralData.h)."""
 
     def __init__(self):
         self._x, self._y, self._z = [], [], []
+        self._data, self._err = np.zeros(0), np.zeros(0)
+
+    def SetDataAndErrors(self, D, E):
+        """GeneralData.h:117-126: data and errors of equal length."""
+        D, E = np.array(D, dtype=float), np.array(E, dtype=float)
+        if D.size != E.size:
+            raise FatalException("Data and Errors do not have the same size !")
+        self._data, self._err = D, E
+
+    def SetErrors(self, E):
+        E = np.array(E, dtype=float)
+        if E.size != self._data.size:
+            raise FatalException("Data and Errors do not have the same size !")
+        self._err = E
+
+    def GetData(self):
+        return self._data
+
+    def GetErrors(self):
+        return self._err
 
     def AddMeasurementPoint(self, x, y, z):
         self._x.append(float(x))

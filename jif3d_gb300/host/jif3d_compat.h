@@ -88,8 +88,12 @@ class TotalFieldAnomaly : public VectorTransform {
 
 // Rectilinear mesh: origin + cell sizes, corner coordinates as running sums
 // (ModelBase/ThreeDModelBase.cpp:96-113), values z fastest.
+// The cell values are one flat block, z fastest (the reference keeps a
+// boost::multi_array, ThreeDModelBase.h:49-51, 119-128).
 class ThreeDModelBase {
  public:
+  typedef std::vector<double> t3DModelDim;
+  typedef std::vector<double> t3DModelData;
   virtual ~ThreeDModelBase() {}
   void SetMesh(const std::vector<double> &xs, const std::vector<double> &ys,
                const std::vector<double> &zs, double x0, double y0, double z0) {
@@ -100,6 +104,13 @@ class ThreeDModelBase {
     yc_ = Coords(y0, ys);
     zc_ = Coords(z0, zs);
   }
+  // the origin stays, the corners are recomputed (ThreeDModelBase.h:74-90)
+  void SetXCellSizes(const t3DModelDim &v) { xs_ = v, xc_ = Coords(Origin(xc_), v); }
+  void SetYCellSizes(const t3DModelDim &v) { ys_ = v, yc_ = Coords(Origin(yc_), v); }
+  void SetZCellSizes(const t3DModelDim &v) { zs_ = v, zc_ = Coords(Origin(zc_), v); }
+  t3DModelData &SetData() { return data_; }
+  const t3DModelData &GetData() const { return data_; }
+  size_t GetNModelElements() const { return data_.size(); }
   const std::vector<double> &GetXCellSizes() const { return xs_; }
   const std::vector<double> &GetYCellSizes() const { return ys_; }
   const std::vector<double> &GetZCellSizes() const { return zs_; }
@@ -109,6 +120,7 @@ class ThreeDModelBase {
   size_t NCells() const { return xs_.size() * ys_.size() * zs_.size(); }
 
  private:
+  static double Origin(const std::vector<double> &c) { return c.empty() ? 0.0 : c[0]; }
   static std::vector<double> Coords(double o, const std::vector<double> &s) {
     std::vector<double> c(1, o);
     double v = o;
@@ -116,26 +128,28 @@ class ThreeDModelBase {
     return c;
   }
   std::vector<double> xs_, ys_, zs_, xc_, yc_, zc_;
+  t3DModelData data_;
 };
 
 // One cell block plus background layers (ThreeDGravityModel.h:91-104,
 // ThreeDSusceptibilityModel.h:42-55).
 class ThreeDLayeredModel : public ThreeDModelBase {
  public:
-  std::vector<double> &SetValues() { return values_; }
+  std::vector<double> &SetValues() { return SetData(); }
   std::vector<double> &SetBackgroundValues() { return bgv_; }
   std::vector<double> &SetBackgroundThicknesses() { return bgt_; }
   const std::vector<double> &GetBackgroundThicknesses() const { return bgt_; }
   rvec GetModelParameters() const {
-    rvec p(values_.size() + bgv_.size());
-    for (size_t i = 0; i < values_.size(); ++i) p(i) = values_[i];
-    for (size_t i = 0; i < bgv_.size(); ++i) p(values_.size() + i) = bgv_[i];
+    const std::vector<double> &values = GetData();
+    rvec p(values.size() + bgv_.size());
+    for (size_t i = 0; i < values.size(); ++i) p(i) = values[i];
+    for (size_t i = 0; i < bgv_.size(); ++i) p(values.size() + i) = bgv_[i];
     return p;
   }
-  size_t GetNModelParm() const { return values_.size() + bgv_.size(); }
+  size_t GetNModelParm() const { return GetData().size() + bgv_.size(); }
 
  private:
-  std::vector<double> values_, bgv_, bgt_;
+  std::vector<double> bgv_, bgt_;
 };
 class ThreeDGravityModel : public ThreeDLayeredModel {};
 class ThreeDSusceptibilityModel : public ThreeDLayeredModel {};
@@ -144,10 +158,11 @@ class ThreeDSusceptibilityModel : public ThreeDLayeredModel {};
 // (ThreeDMagnetizationModel.h:53-70).
 class ThreeDMagnetizationModel : public ThreeDModelBase {
  public:
-  std::vector<double> &SetMagnetization_X() { return mx_; }
+  std::vector<double> &SetMagnetization_X() { return SetData(); }
   std::vector<double> &SetMagnetization_Y() { return my_; }
   std::vector<double> &SetMagnetization_Z() { return mz_; }
   rvec GetModelParameters() const {
+    const std::vector<double> &mx_ = GetData();
     const size_t n = mx_.size();
     rvec p(3 * n);
     for (size_t i = 0; i < n; ++i) {
@@ -157,10 +172,10 @@ class ThreeDMagnetizationModel : public ThreeDModelBase {
     }
     return p;
   }
-  size_t GetNModelParm() const { return 3 * mx_.size(); }
+  size_t GetNModelParm() const { return 3 * GetData().size(); }
 
  private:
-  std::vector<double> mx_, my_, mz_;
+  std::vector<double> my_, mz_;
 };
 
 class GeneralData {

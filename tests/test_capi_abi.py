@@ -71,16 +71,18 @@ def test_null_context_is_rejected(lib):
 
 
 def test_cpp_implementation_header_compiles():
-    """The C++ implementation objects compile against the stand-in jif3D
-    declarations (no GPU needed: syntax and template instantiation only)."""
+    """The C++ implementation objects and the refiner compile against the
+    stand-in jif3D declarations (no GPU needed: syntax and template
+    instantiation only)."""
     import shutil
     import subprocess
     if not shutil.which("g++"):
         pytest.skip("g++ not available")
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror",
-                        "-I", os.path.join(root, "include"),
-                        "-I", os.path.join(root, "jif3d_gb300", "host"),
-                        os.path.join(root, "tests", "cpp", "host_adapter_check.cpp")],
-                       capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr
+    for src in ("host_adapter_check.cpp", "refiner_check.cpp"):
+        r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-Wextra", "-Werror",
+                            "-I", os.path.join(root, "include"),
+                            "-I", os.path.join(root, "jif3d_gb300", "host"),
+                            os.path.join(root, "tests", "cpp", src)],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, (src, r.stderr)

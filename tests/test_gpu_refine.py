@@ -269,3 +269,57 @@ def test_kernel_paths(ctx, oracle_lib, case):
     for i in range(2):
         assert same_bits(dF[i].cpu().numpy(), oracle_project(oracle_lib, s, f, C[i], 1, 0))
         assert same_bits(dOut[i].cpu().numpy(), oracle_combine(oracle_lib, s, f, Fg[i], 1, 0))
+
+
+def test_cpp_refiner(oracle_lib, tmp_path):
+    """jif3D::GB300ModelRefiner (the C++ drop-in for ModelRefiner) driven as
+    ThreeDModelObjective drives its refiner: refined axes, projected values
+    and combined gradient against the oracle, bit for bit; a copied refiner
+    gives the same gradient; a zero-size last cell throws FatalException."""
+    import os
+    import subprocess
+    from jif3d_gb300 import build as B
+    B.build()
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    exe = str(tmp_path / "refiner_check")
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(root, "include"),
+                        "-I", os.path.join(root, "jif3d_gb300", "host"),
+                        os.path.join(here, "cpp", "refiner_check.cpp"),
+                        "-L", os.path.dirname(B.LIB), "-ljif3d_gb300",
+                        "-Wl,-rpath," + os.path.dirname(B.LIB), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    O = oracle_lib
+    rng = np.random.default_rng(70)
+    cs = [rng.integers(10, 30, 5).astype(float) + 0.25, rng.integers(10, 30, 4).astype(float),
+          rng.integers(5, 20, 6) * 1.1]
+    origin = (-3.0, 2.5, 0.0)
+    cc = [O.corners(o, c) for o, c in zip(origin, cs)]
+    refs = [np.sort(rng.uniform(c[0], c[-1], 9).round(1)) for c in cc]
+    fs = [O.refine_axis(c, s_, r_) for c, s_, r_ in zip(cc, cs, refs)]
+    values = rng.normal(size=int(np.prod([c.size for c in cs])))
+    fgrad = rng.normal(size=int(np.prod([f.size for f in fs])))
+    fgrad[::5] = -0.0
+    with open(tmp_path / "p.txt", "w") as f:
+        parts = [repr(float(v)) for v in origin]
+        for v in (*cs, *refs, values, fgrad):
+            parts += [str(len(v))] + [repr(float(x)) for x in v]
+        f.write(" ".join(parts))
+    r = subprocess.run([exe, str(tmp_path / "p.txt"), str(tmp_path / "o.txt")],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    out, exc = {}, False
+    for line in open(tmp_path / "o.txt"):
+        p = line.split()
+        if p[:2] == ["exception", "ok"]:
+            exc = True
+            continue
+        out[p[0]] = np.array([float(v) for v in p[2:]])
+    for a, name in enumerate(("xsizes", "ysizes", "zsizes")):
+        assert same_bits(out[name], fs[a])
+    assert same_bits(out["fine"], O.refine_project(cs, fs, values))
+    ref_grad = O.refine_combine(cs, fs, fgrad)
+    assert same_bits(out["coarse_grad"], ref_grad)
+    assert same_bits(out["copy_grad"], ref_grad)
+    assert exc
