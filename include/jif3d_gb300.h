@@ -247,6 +247,53 @@ int j3g_batched_forward(j3g_context *ctx, int nmodels, const double *h_models, d
 int j3g_batched_lqderivative(j3g_context *ctx, int nmodels, const double *h_models,
                              const double *h_misfits, double *h_grads);
 
+/* ---- NetCDF files: jif3D's on-disk data and models ---------------------------
+ * jif3D stores data and models with netCDF (Gravity/ReadWriteGravityData.cpp,
+ * Magnetics/ReadWriteMagneticData.cpp, ModelBase/NetCDFModelTools.cpp); this
+ * library reads and writes those files itself, with no NetCDF or HDF5
+ * library.  Readers take NetCDF classic files (CDF-1, CDF-2, CDF-5) and
+ * netCDF-4 files (HDF5: compact or contiguous datasets, compact or
+ * symbol-table groups, as netCDF-4 writes jif3D's files); chunked datasets
+ * are J3G_ERR_ARG with a message.  The writer produces CDF-2 (64-bit offset)
+ * files, which jif3D's netCDF-C++ reads like its own.  Values are exchanged
+ * as double.  Host only: no context and no GPU.  On failure the message is
+ * j3g_nc_last_error() (per thread). */
+typedef struct j3g_ncfile j3g_ncfile;
+typedef struct j3g_ncwriter j3g_ncwriter;
+enum { J3G_NC_BYTE = 1, J3G_NC_CHAR = 2, J3G_NC_SHORT = 3, J3G_NC_INT = 4, J3G_NC_FLOAT = 5,
+       J3G_NC_DOUBLE = 6 };
+const char *j3g_nc_last_error(void);
+/* Read a whole file (NcFile(filename, NcFile::read)). */
+int j3g_nc_open(const char *path, j3g_ncfile **file);
+int j3g_nc_close(j3g_ncfile *file);
+/* 1, 2, 5: classic CDF-1 / CDF-2 / CDF-5; 4: netCDF-4 (HDF5). */
+int j3g_nc_format(const j3g_ncfile *file, int *format);
+int j3g_nc_nvars(const j3g_ncfile *file, int *nvars);
+int j3g_nc_var_name(const j3g_ncfile *file, int index, int capacity, char *name);
+/* Shape of a variable (getVar(name).getDims()); J3G_ERR_ARG if it is absent. */
+int j3g_nc_var_shape(const j3g_ncfile *file, const char *var, int capacity, int *ndims,
+                     long long *shape);
+/* All values of a variable, row-major, as double (ReadVec, Global/NetCDFTools.h). */
+int j3g_nc_read_var(const j3g_ncfile *file, const char *var, long long count, double *values);
+/* Length of a dimension (getDim(name).getSize()). */
+int j3g_nc_dim_len(const j3g_ncfile *file, const char *dim, long long *len);
+/* A text attribute of a variable, or of the file when var is NULL. */
+int j3g_nc_text_att(const j3g_ncfile *file, const char *var, const char *att, int capacity,
+                    char *value);
+/* Writer (NcFile(filename, NcFile::replace), addDim, addVar, putAtt, putVar);
+ * the file is written by j3g_nc_close_writer, which also frees the writer. */
+int j3g_nc_create(const char *path, j3g_ncwriter **writer);
+int j3g_nc_def_dim(j3g_ncwriter *writer, const char *name, long long len);
+int j3g_nc_def_var(j3g_ncwriter *writer, const char *name, int type, int ndims,
+                   const char *const *dims);
+int j3g_nc_put_text_att(j3g_ncwriter *writer, const char *var, const char *name,
+                        const char *value);
+int j3g_nc_put_var(j3g_ncwriter *writer, const char *var, long long count,
+                   const double *values);
+int j3g_nc_close_writer(j3g_ncwriter *writer);
+/* Free a writer without writing its file. */
+int j3g_nc_discard_writer(j3g_ncwriter *writer);
+
 /* Block until the context's stream is idle; reports J3G_ERR_CUDA if a
  * bounded wait inside a tensor-core kernel expired since the last check. */
 int j3g_synchronize(j3g_context *ctx);

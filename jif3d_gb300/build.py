@@ -28,7 +28,9 @@ def nvcc() -> str:
 
 
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    """CUDA translation units and the host-only C++ ones (NetCDF I/O)."""
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC)
+                  if f.endswith(".cu") or f.endswith(".cpp"))
 
 
 def _flags():

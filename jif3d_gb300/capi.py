@@ -73,6 +73,24 @@ SIGNATURES = {
     "j3g_refine_combine_device": (_I, [_VP, _I, _VP, _VP]),
     "j3g_refine_project": (_I, [_VP, _I, _P, _P]),
     "j3g_refine_combine": (_I, [_VP, _I, _P, _P]),
+    "j3g_nc_last_error": (ctypes.c_char_p, []),
+    "j3g_nc_open": (_I, [ctypes.c_char_p, ctypes.POINTER(_VP)]),
+    "j3g_nc_close": (_I, [_VP]),
+    "j3g_nc_format": (_I, [_VP, ctypes.POINTER(_I)]),
+    "j3g_nc_nvars": (_I, [_VP, ctypes.POINTER(_I)]),
+    "j3g_nc_var_name": (_I, [_VP, _I, _I, ctypes.c_char_p]),
+    "j3g_nc_var_shape": (_I, [_VP, ctypes.c_char_p, _I, ctypes.POINTER(_I),
+                              ctypes.POINTER(_LL)]),
+    "j3g_nc_read_var": (_I, [_VP, ctypes.c_char_p, _LL, _P]),
+    "j3g_nc_dim_len": (_I, [_VP, ctypes.c_char_p, ctypes.POINTER(_LL)]),
+    "j3g_nc_text_att": (_I, [_VP, ctypes.c_char_p, ctypes.c_char_p, _I, ctypes.c_char_p]),
+    "j3g_nc_create": (_I, [ctypes.c_char_p, ctypes.POINTER(_VP)]),
+    "j3g_nc_def_dim": (_I, [_VP, ctypes.c_char_p, _LL]),
+    "j3g_nc_def_var": (_I, [_VP, ctypes.c_char_p, _I, _I, ctypes.POINTER(ctypes.c_char_p)]),
+    "j3g_nc_put_text_att": (_I, [_VP, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]),
+    "j3g_nc_put_var": (_I, [_VP, ctypes.c_char_p, _LL, _P]),
+    "j3g_nc_close_writer": (_I, [_VP]),
+    "j3g_nc_discard_writer": (_I, [_VP]),
     "j3g_probe_fp64": (_I, [_VP, _P]),
     "j3g_probe_math": (_I, [_I, _I]),
     "j3g_forward_noalloc": (_I, [_I, _I, _I, _I, _VP, _VP, _VP, _I, _VP, _VP, _VP, _D, _D, _D,
@@ -131,6 +149,134 @@ def refine_axis(coarse_coords, coarse_sizes, ref_coords):
         raise J3GError(rc_, "Negative cell size in model refinement" if n.value < 0 else
                        "bad refinement arguments")
     return out[:n.value].copy()
+
+
+NC_INT, NC_FLOAT, NC_DOUBLE = 4, 5, 6
+
+
+def _nc_check(rc):
+    if rc != OK:
+        raise J3GError(rc, (load().j3g_nc_last_error() or b"").decode())
+
+
+def _b(s):
+    return None if s is None else s.encode()
+
+
+class NcFile:
+    """A NetCDF file read whole by the library (classic or netCDF-4); host only."""
+
+    def __init__(self, path):
+        self._lib = load()
+        h = _VP()
+        _nc_check(self._lib.j3g_nc_open(os.fsencode(path), ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.j3g_nc_close(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def format(self):
+        f = _I()
+        _nc_check(self._lib.j3g_nc_format(self._h, ctypes.byref(f)))
+        return f.value
+
+    def variables(self):
+        n = _I()
+        _nc_check(self._lib.j3g_nc_nvars(self._h, ctypes.byref(n)))
+        out = []
+        for i in range(n.value):
+            buf = ctypes.create_string_buffer(1024)
+            _nc_check(self._lib.j3g_nc_var_name(self._h, i, 1024, buf))
+            out.append(buf.value.decode())
+        return out
+
+    def has_var(self, name):
+        nd, shp = _I(), (_LL * 32)()
+        return self._lib.j3g_nc_var_shape(self._h, _b(name), 32, ctypes.byref(nd), shp) == OK
+
+    def shape(self, name):
+        nd, shp = _I(), (_LL * 32)()
+        _nc_check(self._lib.j3g_nc_var_shape(self._h, _b(name), 32, ctypes.byref(nd), shp))
+        return tuple(int(x) for x in shp[:nd.value])
+
+    def read(self, name):
+        shape = self.shape(name)
+        out = np.zeros(int(np.prod(shape)) if shape else 1)
+        _nc_check(self._lib.j3g_nc_read_var(self._h, _b(name), out.size, _ptr(out)))
+        return out.reshape(shape) if shape else out
+
+    def dim(self, name):
+        n = _LL()
+        _nc_check(self._lib.j3g_nc_dim_len(self._h, _b(name), ctypes.byref(n)))
+        return n.value
+
+    def has_dim(self, name):
+        n = _LL()
+        return self._lib.j3g_nc_dim_len(self._h, _b(name), ctypes.byref(n)) == OK
+
+    def att(self, var, name):
+        """A text attribute of variable ``var`` (None: of the file), or None."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        rc = self._lib.j3g_nc_text_att(self._h, _b(var), _b(name), 1 << 16, buf)
+        return buf.value.decode() if rc == OK else None
+
+
+class NcWriter:
+    """A CDF-2 NetCDF file written by the library when closed; host only."""
+
+    def __init__(self, path):
+        self._lib = load()
+        h = _VP()
+        _nc_check(self._lib.j3g_nc_create(os.fsencode(path), ctypes.byref(h)))
+        self._h = h
+
+    def add_dim(self, name, n):
+        _nc_check(self._lib.j3g_nc_def_dim(self._h, _b(name), int(n)))
+
+    def add_var(self, name, dims=(), type=NC_DOUBLE, values=None, **atts):
+        arr = (ctypes.c_char_p * max(1, len(dims)))(*[_b(d) for d in dims])
+        _nc_check(self._lib.j3g_nc_def_var(self._h, _b(name), type, len(dims), arr))
+        for k, v in atts.items():
+            self.put_att(name, k, v)
+        if values is not None:
+            self.put(name, values)
+
+    def put_att(self, var, name, value):
+        _nc_check(self._lib.j3g_nc_put_text_att(self._h, _b(var), _b(name), _b(str(value))))
+
+    def put(self, name, values):
+        v = _f64(values).reshape(-1)
+        _nc_check(self._lib.j3g_nc_put_var(self._h, _b(name), v.size, _ptr(v)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            h, self._h = self._h, None
+            _nc_check(self._lib.j3g_nc_close_writer(h))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, exc_type, *exc):
+        if exc_type is None:
+            self.close()
+        elif getattr(self, "_h", None):  # drop the half-defined file
+            h, self._h = self._h, None
+            self._lib.j3g_nc_discard_writer(h)
 
 
 class Context:

@@ -47,25 +47,56 @@ class ThreeDModelBase:
         self._data = np.zeros((0, 0, 0))
         self._bg_values = np.zeros(0)
         self._bg_thick = np.zeros(0)
+        # corner coordinates set as such (SetXCoordinates, e.g. read from a
+        # file) are kept as given; otherwise they are the running sums
+        self._corners = [None, None, None]
 
     # mesh -------------------------------------------------------------------
     def SetMeshSize(self, nx, ny, nz):
         self._xs = np.resize(self._xs, nx).astype(float)
         self._ys = np.resize(self._ys, ny).astype(float)
         self._zs = np.resize(self._zs, nz).astype(float)
+        self._corners = [None, None, None]
         self._data = np.zeros((nx, ny, nz))
 
     def SetXCellSizes(self, v):
         self._xs = np.array(v, dtype=float)
+        self._corners[0] = None
 
     def SetYCellSizes(self, v):
         self._ys = np.array(v, dtype=float)
+        self._corners[1] = None
 
     def SetZCellSizes(self, v):
         self._zs = np.array(v, dtype=float)
+        self._corners[2] = None
+
+    def _set_corners(self, axis, c):
+        """ThreeDModelBase::SetXCoordinates (ThreeDModelBase.h:92-108): the
+        corners as given, the sizes their differences (CalcSizes)."""
+        c = np.array(c, dtype=float)
+        self._corners[axis] = c
+        self._origin[axis] = c[0] if c.size else 0.0
+        sizes = np.diff(c)
+        if axis == 0:
+            self._xs = sizes
+        elif axis == 1:
+            self._ys = sizes
+        else:
+            self._zs = sizes
+
+    def SetXCoordinates(self, c):
+        self._set_corners(0, c)
+
+    def SetYCoordinates(self, c):
+        self._set_corners(1, c)
+
+    def SetZCoordinates(self, c):
+        self._set_corners(2, c)
 
     def SetOrigin(self, x, y, z):
         self._origin = np.array([x, y, z], dtype=float)
+        self._corners = [None, None, None]
 
     def GetXCellSizes(self):
         return self._xs
@@ -89,13 +120,16 @@ class ThreeDModelBase:
         return c
 
     def GetXCoordinates(self):
-        return self._coords(self._origin[0], self._xs)
+        c = self._corners[0]
+        return c.copy() if c is not None else self._coords(self._origin[0], self._xs)
 
     def GetYCoordinates(self):
-        return self._coords(self._origin[1], self._ys)
+        c = self._corners[1]
+        return c.copy() if c is not None else self._coords(self._origin[1], self._ys)
 
     def GetZCoordinates(self):
-        return self._coords(self._origin[2], self._zs)
+        c = self._corners[2]
+        return c.copy() if c is not None else self._coords(self._origin[2], self._zs)
 
     def GetXOrigin(self):
         return float(self._origin[0])
@@ -142,12 +176,36 @@ class ThreeDGravityModel(ThreeDModelBase):
     SetBackgroundDensities = ThreeDModelBase.SetBackgroundValues
     GetBackgroundDensities = ThreeDModelBase.GetBackgroundValues
 
+    def WriteNetCDF(self, filename):
+        """Gravity/ThreeDGravityModel.cpp:75-101: Density (kg/m3) and the
+        background layers."""
+        from . import netcdf
+        netcdf.WriteLayeredModel(self, filename, "Density", "kg/m3", "bg_densities",
+                                 "Background Densities")
+
+    def ReadNetCDF(self, filename):
+        """Gravity/ThreeDGravityModel.cpp:103-162 (g/cm3 files are scaled to kg/m3)."""
+        from . import netcdf
+        netcdf.ReadLayeredModel(self, filename, "Density", "kg/m3", "bg_densities",
+                                old_units="g/cm3", old_factor=1000.0)
+
 
 class ThreeDSusceptibilityModel(ThreeDModelBase):
     SetSusceptibilities = ThreeDModelBase.SetData
     GetSusceptibilities = ThreeDModelBase.GetData
     SetBackgroundSusceptibilities = ThreeDModelBase.SetBackgroundValues
     GetBackgroundSusceptibilities = ThreeDModelBase.GetBackgroundValues
+
+    def WriteNetCDF(self, filename):
+        """Magnetics/ThreeDSusceptibilityModel.h:112-148 (units " ")."""
+        from . import netcdf
+        netcdf.WriteLayeredModel(self, filename, "Susceptibility", " ",
+                                 "bg_susceptibilities", "Background Susceptibilities")
+
+    def ReadNetCDF(self, filename):
+        """Magnetics/ThreeDSusceptibilityModel.h:150-190."""
+        from . import netcdf
+        netcdf.ReadLayeredModel(self, filename, "Susceptibility", " ", "bg_susceptibilities")
 
 
 class ThreeDMagnetizationModel(ThreeDModelBase):
@@ -186,6 +244,16 @@ class ThreeDMagnetizationModel(ThreeDModelBase):
     def GetModelParameters(self):
         return np.concatenate([self._data.reshape(-1), self._my.reshape(-1),
                                self._mz.reshape(-1)])
+
+    def WriteNetCDF(self, filename):
+        """Magnetics/ThreeDMagnetizationModel.cpp:28-103: Mx, My, Mz (A/m)."""
+        from . import netcdf
+        netcdf.WriteMagnetizationModel(self, filename)
+
+    def ReadNetCDF(self, filename):
+        """Magnetics/ThreeDMagnetizationModel.cpp:105-145."""
+        from . import netcdf
+        netcdf.ReadMagnetizationModel(self, filename)
 
     def GetNModelParm(self):
         return 3 * self._data.size
@@ -238,20 +306,42 @@ class GeneralData:
         self._x, self._y, self._z = [], [], []
 
 
+    # ReadNetCDF / WriteNetCDF of the data classes (Gravity/ScalarGravityData.cpp:16-38
+    # and the like): positions, data and errors through the format's functions
+    _read = _save = None
+
+    def ReadNetCDF(self, filename):
+        from . import netcdf
+        Data, PosX, PosY, PosZ, Error = getattr(netcdf, self._read)(filename)
+        self.ClearMeasurementPoints()
+        for x, y, z in zip(PosX, PosY, PosZ):
+            self.AddMeasurementPoint(x, y, z)
+        self.SetDataAndErrors(Data, Error if len(Error) == len(Data) else np.zeros(len(Data)))
+
+    def WriteNetCDF(self, filename):
+        from . import netcdf
+        getattr(netcdf, self._save)(filename, self.GetData(), self.GetMeasPosX(),
+                                    self.GetMeasPosY(), self.GetMeasPosZ(), self.GetErrors())
+
+
 class ScalarGravityData(GeneralData):
     ModelType = ThreeDGravityModel
+    _read, _save = "ReadScalarGravityMeasurements", "SaveScalarGravityMeasurements"
 
 
 class TensorGravityData(GeneralData):
     ModelType = ThreeDGravityModel
+    _read, _save = "ReadTensorGravityMeasurements", "SaveTensorGravityMeasurements"
 
 
 class TotalFieldMagneticData(GeneralData):
     ModelType = ThreeDSusceptibilityModel
+    _read, _save = "ReadTotalFieldMagneticMeasurements", "SaveTotalFieldMagneticMeasurements"
 
 
 class ThreeComponentMagneticData(GeneralData):
     ModelType = ThreeDMagnetizationModel
+    _read, _save = "ReadMagneticComponentMeasurements", "SaveMagneticComponentMeasurements"
 
 
 # ---------------------------------------------------------------------------
@@ -379,7 +469,9 @@ class GB300GravMagImplementation:
                getattr(self.Transform, "declination", 0.0),
                Model.GetXOrigin(), Model.GetYOrigin(), Model.GetZOrigin(),
                Model.GetXCellSizes().tobytes(), Model.GetYCellSizes().tobytes(),
-               Model.GetZCellSizes().tobytes(), Model.GetBackgroundThicknesses().tobytes(),
+               Model.GetZCellSizes().tobytes(), Model.GetXCoordinates().tobytes(),
+               Model.GetYCoordinates().tobytes(), Model.GetZCoordinates().tobytes(),
+               Model.GetBackgroundThicknesses().tobytes(),
                Data.GetMeasPosX().tobytes(), Data.GetMeasPosY().tobytes(),
                Data.GetMeasPosZ().tobytes())
         if key != self._key:

@@ -6,6 +6,12 @@
 * simpeg_mag.json -- the SimPEG comparison values that the reference's
   Magnetics/test_MagneticCalculation.cpp:164-217 checks against
   (jif3D/magx.simpeg, magy, magz, magt: Bx, By, Bz, TFA in nT).
+* tutorial5_gravdata.nc, tutorial5_magdata.nc -- the gravity and total-field
+  magnetic data files of jif3D's Tutorial 5 (netCDF-4 / HDF5 files written by
+  jif3D), copied unchanged, and netcdf_tutorial.json -- the values the
+  tutorial notebook printed after reading magdata.nc with netCDF4 (station
+  spacing and the range of MeasPosX / MeasPosY), taken from the notebook's
+  stored output.
 
 Run here, where the reference sources exist:
     python tests/golden/make_golden.py [path/to/jif3D]
@@ -85,6 +91,39 @@ def main():
     with open(os.path.join(HERE, "simpeg_mag.json"), "w") as f:
         json.dump(sim, f)
     print("wrote", len(out), "box cases and", len(sim["x"]), "SimPEG stations")
+    tutorial(os.path.join(ref_root, "Tutorial", "Tutorial5"))
+
+
+def tutorial(folder):
+    import hashlib
+    import re
+    import shutil
+    meta = {"source": "jif3D Tutorial/Tutorial5 (gravdata.nc, magdata.nc, Tutorial5.ipynb)",
+            "files": {}}
+    for name in ("gravdata.nc", "magdata.nc"):
+        dst = os.path.join(HERE, "tutorial5_" + name)
+        shutil.copyfile(os.path.join(folder, name), dst)
+        with open(dst, "rb") as f:
+            meta["files"][os.path.basename(dst)] = hashlib.sha256(f.read()).hexdigest()
+    with open(os.path.join(folder, "Tutorial5.ipynb")) as f:
+        nb = json.load(f)
+    printed = None
+    for cell in nb["cells"]:
+        src = "".join(cell.get("source", []))
+        if 'Dataset("magdata.nc"' in src:
+            printed = "".join("".join(o.get("text", [])) for o in cell.get("outputs", []))
+    if printed is None:
+        raise SystemExit("notebook cell reading magdata.nc not found")
+    keys = {"Data spacing": "spacing", "Minimum x": "min_x", "Maximum x": "max_x",
+            "Minimum y": "min_y", "Maximum y": "max_y"}
+    meta["magdata_printed"] = {}
+    for line in printed.splitlines():
+        m = re.match(r"\s*([A-Za-z ]+):\s*(\S+)", line)
+        if m and m.group(1).strip() in keys:
+            meta["magdata_printed"][keys[m.group(1).strip()]] = m.group(2)
+    with open(os.path.join(HERE, "netcdf_tutorial.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    print("copied the Tutorial 5 data files;", meta["magdata_printed"])
 
 
 if __name__ == "__main__":
