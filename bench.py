@@ -224,6 +224,37 @@ def measure_refinement(s, nmod, steps, stream, flush, local, peaks):
     return out
 
 
+def measure_netcdf(s, data):
+    """Host throughput of the library's NetCDF writer and reader on the
+    workload's files: the density model (131,072 cells) and the FTG data of
+    the 1024 stations, written as CDF-2 and read back (MB/s of file bytes)."""
+    import tempfile
+    from jif3d_gb300 import gravmag as G, netcdf as N
+    M = G.ThreeDGravityModel()
+    M.SetMeshSize(*s.shape)
+    M.SetXCellSizes(s.xsize)
+    M.SetYCellSizes(s.ysize)
+    M.SetZCellSizes(s.zsize)
+    M.SetData()[...] = s.model[:s.ngrid].reshape(s.shape)
+    st = s.stations
+    with tempfile.TemporaryDirectory() as tmp:
+        out = {}
+        for name, write, read in (
+                ("model", lambda f: M.WriteNetCDF(f), lambda f: G.ThreeDGravityModel().ReadNetCDF(f)),
+                ("ftg_data", lambda f: N.SaveTensorGravityMeasurements(
+                    f, data, st[:, 0], st[:, 1], st[:, 2], np.ones_like(data)),
+                 lambda f: N.ReadTensorGravityMeasurements(f))):
+            f = os.path.join(tmp, name + ".nc")
+            t0 = time.perf_counter()
+            write(f)
+            t1 = time.perf_counter()
+            read(f)
+            t2 = time.perf_counter()
+            mb = os.path.getsize(f) / 1e6
+            out[name] = {"file_mb": mb, "write_mbs": mb / (t1 - t0), "read_mbs": mb / (t2 - t1)}
+    return out
+
+
 def run_batched(args, rank, world, local):
     import torch
     from jif3d_gb300 import capi, workloads as W
@@ -397,6 +428,8 @@ def run_batched(args, rank, world, local):
             "hbm_peak_gbs": peaks["hbm_gbs"]}
     ctx.close()
     refinement = measure_refinement(s, nmod, args.steps, stream, flush, local, peaks)
+    ftg = data[0].view(n, 10)[:, 1:].reshape(-1).cpu().numpy()
+    netcdf_io = measure_netcdf(s, ftg) if rank == 0 else None
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -417,7 +450,7 @@ def run_batched(args, rank, world, local):
         "step": "one CUDA graph per step (batched forward, weighted misfit, batched "
                 "adjoint: %d library kernels + 2 torch kernels), replayed" % launches_per_step,
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "clocks": clk,
-        "refinement": refinement,
+        "refinement": refinement, "netcdf": netcdf_io,
     }
 
 
