@@ -39,10 +39,11 @@ UNIT = "Mcell*station/s"
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 SIGMA_GZ, SIGMA_U = 1e-8, 1e-9
 
-# FP64 flop-equivalents per joint node evaluation: 21 add/mul + sqrt + 3 ln +
-# 4 atan2 + 7 accumulation FMA with the ncu-measured weights sqrt 13, ln 44,
-# atan2 59.5 (profiles/fp64_weights.md).
-FP64_FLOP_PER_JOINT_NODE = 418.0
+# FP64 flops per joint node evaluation (an FMA counts 2): 21 add/mul + sqrt +
+# 3 flog + 2 fatan2 + 1 fatan2_pair + 7 accumulation FMA, with the weights
+# measured by ncu on the probe kernels: sqrt 13, flog 21, fatan2 36, pair 42
+# (profiles/fp64_weights.md); the node kernels' own counters give 223 / 214.
+FP64_FLOP_PER_JOINT_NODE = 225.0
 
 
 def parse():
