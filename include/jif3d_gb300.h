@@ -246,6 +246,19 @@ int j3g_batched_lqderivative_device(j3g_context *ctx, int nmodels, const double 
 int j3g_batched_forward(j3g_context *ctx, int nmodels, const double *h_models, double *h_data);
 int j3g_batched_lqderivative(j3g_context *ctx, int nmodels, const double *h_models,
                              const double *h_misfits, double *h_grads);
+/* Pipelined host-buffer forms: the call queues the copy of its inputs in,
+ * the product and the copy of its output back, and returns a ticket; the
+ * copies run on two streams of the context's own (in, out), so they overlap
+ * the products of the calls before and after.  j3g_batched_wait(ticket)
+ * blocks until that call's output is in host memory.  Up to three calls are
+ * in flight (a fourth waits for the first); the host buffers must stay
+ * valid and unchanged until the call is waited for, and page-locked host
+ * buffers are needed for the copies to overlap. */
+int j3g_batched_forward_async(j3g_context *ctx, int nmodels, const double *h_models,
+                              double *h_data, long long *ticket);
+int j3g_batched_lqderivative_async(j3g_context *ctx, int nmodels, const double *h_models,
+                                   const double *h_misfits, double *h_grads, long long *ticket);
+int j3g_batched_wait(j3g_context *ctx, long long ticket);
 
 /* ---- NetCDF files: jif3D's on-disk data and models ---------------------------
  * jif3D stores data and models with netCDF (Gravity/ReadWriteGravityData.cpp,

@@ -56,6 +56,9 @@ SIGNATURES = {
     "j3g_batched_lqderivative_device": (_I, [_VP, _I, _VP, _VP, _VP]),
     "j3g_batched_forward": (_I, [_VP, _I, _P, _P]),
     "j3g_batched_lqderivative": (_I, [_VP, _I, _P, _P, _P]),
+    "j3g_batched_forward_async": (_I, [_VP, _I, _P, _P, ctypes.POINTER(_LL)]),
+    "j3g_batched_lqderivative_async": (_I, [_VP, _I, _P, _P, _P, ctypes.POINTER(_LL)]),
+    "j3g_batched_wait": (_I, [_VP, _LL]),
     "j3g_launch_count": (_I, [_VP, ctypes.POINTER(_LL)]),
     "j3g_set_timing": (_I, [_VP, _I]),
     "j3g_get_timing": (_I, [_VP, _I, _P, ctypes.POINTER(_LL)]),
@@ -292,6 +295,7 @@ class Context:
                            " (a CUDA device is required; there is no CPU fallback)")
         self._h = h
         self._keep = []
+        self._inflight = {}
 
     def close(self):
         if getattr(self, "_h", None):
@@ -444,6 +448,41 @@ class Context:
         self._check(self._lib.j3g_batched_lqderivative(self._h, r.shape[0], _ptr(m), _ptr(r),
                                                        _ptr(g)))
         return g
+
+    # pipelined host-buffer products: the arrays are held until the wait
+    def batched_forward_async(self, models, out):
+        s = self.sizes()
+        m = _f64(models).reshape(-1, s["nparm"])
+        d = self._out(out, (m.shape[0], s["nmeas"] * s["dpm"]))
+        t = _LL()
+        self._check(self._lib.j3g_batched_forward_async(self._h, m.shape[0], _ptr(m), _ptr(d),
+                                                        ctypes.byref(t)))
+        self._hold(t.value, (m, d))
+        return t.value
+
+    def batched_lqderivative_async(self, models, misfits, out):
+        s = self.sizes()
+        r = _f64(misfits).reshape(-1, s["nmeas"] * s["dpm"])
+        m = None if models is None else _f64(models).reshape(r.shape[0], s["nparm"])
+        g = self._out(out, (r.shape[0], s["nparm"]))
+        t = _LL()
+        self._check(self._lib.j3g_batched_lqderivative_async(self._h, r.shape[0], _ptr(m),
+                                                             _ptr(r), _ptr(g), ctypes.byref(t)))
+        self._hold(t.value, (m, r, g))
+        return t.value
+
+    def _hold(self, ticket, arrays):
+        """Keep a call's arrays alive until it is waited for; calls three or
+        more tickets older have completed (their ring slot was reused)."""
+        self._inflight[ticket] = arrays
+        for t in [t for t in self._inflight if t <= ticket - 3]:
+            del self._inflight[t]
+
+    def batched_wait(self, ticket):
+        try:
+            self._check(self._lib.j3g_batched_wait(self._h, int(ticket)))
+        finally:
+            self._inflight.pop(int(ticket), None)
 
     @staticmethod
     def _subsets(subsets):

@@ -15,6 +15,8 @@
 #include <cstring>
 #include <new>
 #include <array>
+#include <functional>
+#include <initializer_list>
 #include <map>
 #include <string>
 #include <vector>
@@ -97,6 +99,20 @@ struct j3g_context {
   int cn[3] = {0, 0, 0};
   DevBuf rmaps, rcoarse, rfine;
   RefineMaps rm{};
+
+  // pipelined host-buffer products (j3g_batched_*_async): inputs copied in on
+  // one stream, outputs out on another, the products on the context's stream;
+  // a ring of device slots lets one call's copies overlap another call's work
+  struct Slot {
+    DevBuf in, in2, out;
+    cudaEvent_t h2d = nullptr, done = nullptr, d2h = nullptr;
+    int *flag = nullptr;    // page-locked copy of the tensor-core error flag
+    long long ticket = -1;  // call in flight in this slot, -1 if free
+  };
+  static constexpr int kSlots = 3;
+  Slot slots[kSlots];
+  cudaStream_t h2d_stream = nullptr, d2h_stream = nullptr;
+  long long next_ticket = 0;
 
   // optional per-category kernel timing (j3g_set_timing): event pairs
   // recorded on the context's stream around the dominant launches
@@ -966,6 +982,16 @@ int j3g_destroy(j3g_context *c) {
                     &c->rcoarse, &c->rfine};
   for (DevBuf *b : bufs)
     if (b->p) cudaFree(b->p);
+  for (auto &sl : c->slots) {
+    if (sl.ticket >= 0 && sl.d2h) cudaEventSynchronize(sl.d2h);
+    for (DevBuf *b : {&sl.in, &sl.in2, &sl.out})
+      if (b->p) cudaFree(b->p);
+    for (cudaEvent_t e : {sl.h2d, sl.done, sl.d2h})
+      if (e) cudaEventDestroy(e);
+    if (sl.flag) cudaFreeHost(sl.flag);
+  }
+  if (c->h2d_stream) cudaStreamDestroy(c->h2d_stream);
+  if (c->d2h_stream) cudaStreamDestroy(c->d2h_stream);
   for (auto &t : c->timed) {
     cudaEventDestroy(t.second.first);
     cudaEventDestroy(t.second.second);
@@ -1322,6 +1348,122 @@ int j3g_batched_lqderivative(j3g_context *c, int nmodels, const double *h_models
                               c->stream));
   J3G_CUDA(c, cudaStreamSynchronize(c->stream));
   return check_gemm_flag(c);
+}
+
+namespace {
+// The next slot of the pipeline ring, its previous call complete; the copy
+// streams and events are made on first use.
+int pipeline_slot(j3g_context *c, j3g_context::Slot *&slot) {
+  if (!c->h2d_stream) {
+    J3G_CUDA(c, cudaStreamCreateWithFlags(&c->h2d_stream, cudaStreamNonBlocking));
+    J3G_CUDA(c, cudaStreamCreateWithFlags(&c->d2h_stream, cudaStreamNonBlocking));
+  }
+  slot = &c->slots[c->next_ticket % j3g_context::kSlots];
+  if (!slot->h2d) {
+    J3G_CUDA(c, cudaEventCreateWithFlags(&slot->h2d, cudaEventDisableTiming));
+    J3G_CUDA(c, cudaEventCreateWithFlags(&slot->done, cudaEventDisableTiming));
+    J3G_CUDA(c, cudaEventCreateWithFlags(&slot->d2h, cudaEventDisableTiming));
+    J3G_CUDA(c, cudaMallocHost(&slot->flag, sizeof(int)));
+  }
+  if (slot->ticket >= 0) {  // the call before in this slot must have finished
+    J3G_CUDA(c, cudaEventSynchronize(slot->d2h));
+    slot->ticket = -1;
+  }
+  return J3G_OK;
+}
+
+// Queue the copies around a product: inputs (host -> slot buffers) on the
+// H2D stream, the product on the context's stream once they are in, the
+// output back on the D2H stream once the product is done.
+struct PipeCopy {
+  const double *host;
+  DevBuf *dev;
+  size_t n;
+};
+int pipeline_run(j3g_context *c, j3g_context::Slot *slot, std::initializer_list<PipeCopy> ins,
+                 double *h_out, size_t n_out, long long *ticket,
+                 const std::function<int(void)> &product) {
+  for (const PipeCopy &in : ins) {
+    if (!in.host) continue;
+    J3G_TRY(ensure(c, *in.dev, sizeof(double) * in.n));
+    J3G_CUDA(c, cudaMemcpyAsync(in.dev->p, in.host, sizeof(double) * in.n,
+                                cudaMemcpyHostToDevice, c->h2d_stream));
+  }
+  J3G_TRY(ensure(c, slot->out, sizeof(double) * n_out));
+  J3G_CUDA(c, cudaEventRecord(slot->h2d, c->h2d_stream));
+  J3G_CUDA(c, cudaStreamWaitEvent(c->stream, slot->h2d, 0));
+  J3G_TRY(product());
+  J3G_CUDA(c, cudaEventRecord(slot->done, c->stream));
+  J3G_CUDA(c, cudaStreamWaitEvent(c->d2h_stream, slot->done, 0));
+  J3G_CUDA(c, cudaMemcpyAsync(h_out, slot->out.p, sizeof(double) * n_out, cudaMemcpyDeviceToHost,
+                              c->d2h_stream));
+  // the error flag of the bounded waits, as it stands after this product
+  *slot->flag = 0;
+  if (c->gerr.p)
+    J3G_CUDA(c, cudaMemcpyAsync(slot->flag, c->gerr.p, sizeof(int), cudaMemcpyDeviceToHost,
+                                c->d2h_stream));
+  J3G_CUDA(c, cudaEventRecord(slot->d2h, c->d2h_stream));
+  slot->ticket = c->next_ticket++;
+  if (ticket) *ticket = slot->ticket;
+  return J3G_OK;
+}
+}  // namespace
+
+int j3g_batched_forward_async(j3g_context *c, int nmodels, const double *h_models,
+                              double *h_data, long long *ticket) {
+  if (!c || nmodels < 1 || !h_models || !h_data)
+    return fail(c, J3G_ERR_ARG, "bad batched arguments");
+  cudaSetDevice(c->device);
+  J3G_TRY(check_stored(c));
+  j3g_context::Slot *slot;
+  J3G_TRY(pipeline_slot(c, slot));
+  const size_t nm = (size_t)nmodels * c->nparm(), nd = (size_t)nmodels * c->nmeas * c->dpm();
+  return pipeline_run(c, slot, {{h_models, &slot->in, nm}}, h_data, nd, ticket, [&]() {
+    return batched_forward_impl(c, nmodels, ptr<double>(slot->in), ptr<double>(slot->out),
+                                nullptr);
+  });
+}
+
+int j3g_batched_lqderivative_async(j3g_context *c, int nmodels, const double *h_models,
+                                   const double *h_misfits, double *h_grads, long long *ticket) {
+  if (!c || nmodels < 1 || !h_misfits || !h_grads)
+    return fail(c, J3G_ERR_ARG, "bad batched arguments");
+  cudaSetDevice(c->device);
+  J3G_TRY(check_stored(c));
+  const bool needs_models =
+      c->transform == J3G_T_FTG_INVARIANT || c->transform == J3G_T_TOTAL_FIELD;
+  if (needs_models && !h_models) return fail(c, J3G_ERR_ARG, "this transform needs the models");
+  j3g_context::Slot *slot;
+  J3G_TRY(pipeline_slot(c, slot));
+  const size_t nm = (size_t)nmodels * c->nparm(), nd = (size_t)nmodels * c->nmeas * c->dpm();
+  return pipeline_run(c, slot,
+                      {{needs_models ? h_models : nullptr, &slot->in, nm},
+                       {h_misfits, &slot->in2, nd}},
+                      h_grads, nm, ticket, [&]() {
+                        return batched_adjoint_impl(
+                            c, nmodels, needs_models ? ptr<double>(slot->in) : nullptr,
+                            ptr<double>(slot->in2), ptr<double>(slot->out));
+                      });
+}
+
+int j3g_batched_wait(j3g_context *c, long long ticket) {
+  if (!c || ticket < 0 || ticket >= c->next_ticket)
+    return fail(c, J3G_ERR_ARG, "no such pipelined call");
+  cudaSetDevice(c->device);
+  // a call that is no longer in its slot has completed (its slot was reused)
+  for (auto &sl : c->slots)
+    if (sl.ticket == ticket) {
+      J3G_CUDA(c, cudaEventSynchronize(sl.d2h));
+      sl.ticket = -1;
+      if (*sl.flag != 0) {
+        const int code = *sl.flag;
+        *sl.flag = 0;
+        cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream);
+        return fail(c, J3G_ERR_CUDA,
+                    "tensor-core pipeline wait expired (code " + std::to_string(code) + ")");
+      }
+    }
+  return J3G_OK;
 }
 
 static void clear_timing(j3g_context *c) {

@@ -131,6 +131,46 @@ def test_batched_host_pinned_outputs(ctx):
         ctx.batched_lqderivative(None, np.zeros((2, t.stations.shape[0])))
 
 
+@pytest.mark.parametrize("kind,transform", [(W.JOINT, W.T_NONE), (W.TENSOR, W.T_FTG_INVARIANT)])
+def test_pipelined_batched_calls(ctx, kind, transform):
+    """The pipelined host-buffer calls give, bit for bit, what the blocking
+    calls give: four forwards in flight (the ring holds three), waits out of
+    order, derivatives with and without the models (the FTG invariant needs
+    them), page-locked and pageable buffers."""
+    import torch
+    s = small_survey(kind, seed=270 + transform, transform=transform, nx=9, ny=8, nz=6,
+                     nmeas=12)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    rng = np.random.default_rng(11)
+    n = s.stations.shape[0]
+    nd = n * s.dpm
+
+    def pinned(shape):
+        return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    batches = [s.model[None, :] * rng.uniform(0.5, 1.5, (3, s.nparm)) for _ in range(4)]
+    outs = [pinned((3, nd)) for _ in batches]
+    tickets = [ctx.batched_forward_async(b, out=o) for b, o in zip(batches, outs)]
+    for t in reversed(tickets):
+        ctx.batched_wait(t)
+    for b, o in zip(batches, outs):
+        assert np.array_equal(o, ctx.batched_forward(b))
+    mis = [rng.normal(size=(3, nd)) for _ in batches]
+    grads = [np.zeros((3, s.nparm)) for _ in batches]  # pageable
+    models = [b if transform != W.T_NONE else None for b in batches]
+    tickets = [ctx.batched_lqderivative_async(m, r, out=g)
+               for m, r, g in zip(models, mis, grads)]
+    t_fwd = ctx.batched_forward_async(batches[0], out=outs[0])
+    ctx.batched_wait(tickets[1])
+    ctx.batched_wait(t_fwd)
+    ctx.batched_wait(tickets[3])
+    ctx.batched_wait(tickets[0])  # its slot was reused: already complete
+    for b, r, g in zip(batches, mis, grads):
+        assert np.array_equal(g, ctx.batched_lqderivative(b, r))
+    with pytest.raises(capi.J3GError):
+        ctx.batched_wait(10 ** 9)
+
+
 def test_stored_is_dropped_on_new_geometry(ctx):
     s = small_survey(W.SCALAR, seed=5)
     W.setup_context(ctx, s)
