@@ -93,14 +93,14 @@ __host__ __device__ inline int kind_mask(int kind) {
          : kind == KIND_MAG_GRADIENT ? KindTraits<KIND_MAG_GRADIENT>::mask
                                     : kTensorMask;
 }
-__host__ __device__ inline int kind_raw(int kind) {
+__host__ __device__ constexpr inline int kind_raw(int kind) {
   return (kind == KIND_SCALAR || kind == KIND_MAG_GRADIENT) ? 1
          : kind == KIND_TENSOR                              ? 9
          : (kind == KIND_MAGNETIC || kind == KIND_MAGNETIZATION) ? 3
                                                             : 10;
 }
 // Virtual components per station.
-__host__ __device__ inline int kind_ncomp(int kind) {
+__host__ __device__ constexpr inline int kind_ncomp(int kind) {
   return kind == KIND_SCALAR ? 1
          : kind == KIND_JOINT ? 7
          : kind == KIND_MAGNETIZATION ? 9
@@ -115,7 +115,7 @@ __host__ __device__ inline bool kind_special(int kind) {
   return kind == KIND_MAG_GRADIENT || kind == KIND_MAGNETIZATION;
 }
 // Slot s of a kind's compact component list -> node component id.
-__host__ __device__ inline int slot_comp(int kind, int s) {
+__host__ __device__ constexpr inline int slot_comp(int kind, int s) {
   return (kind == KIND_SCALAR || kind == KIND_JOINT) ? s : s + 1;
 }
 

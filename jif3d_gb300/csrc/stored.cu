@@ -147,6 +147,13 @@ __global__ void k_transpose16(const uint16_t *__restrict__ in, long long ld_in, 
 constexpr int kChunk = 8192;
 constexpr int kBatch = 8;  // loads in flight per thread in the streaming passes
 static_assert(kChunk % (kT * kBatch) == 0, "chunk must be whole load batches");
+// Column chunk of a split: kChunk, or one load batch per thread (kT * kBatch)
+// when the rows are few and short (residual vectors), so that the grid still
+// has a few blocks per SM.
+inline long long split_chunk(int nrow_pad, long long ld_dst) {
+  const long long blocks = (long long)nrow_pad * ((ld_dst + kChunk - 1) / kChunk);
+  return blocks >= 1024 ? kChunk : kT * kBatch;
+}
 
 __device__ __forceinline__ double scaled_val(const double *src, long long ld_src, int nrow,
                                              long long ncol, const float *colscale, long long r,
@@ -159,14 +166,14 @@ __device__ __forceinline__ double scaled_val(const double *src, long long ld_src
 __global__ void k_row_stats(const double *__restrict__ src, long long ld_src, int nrow,
                             long long ncol, const float *__restrict__ colscale,
                             double *__restrict__ part_max, double *__restrict__ part_sum,
-                            int nchunk) {
+                            int nchunk, int chunk) {
   const long long r = blockIdx.y;
-  const long long c0 = (long long)blockIdx.x * kChunk + threadIdx.x;
+  const long long c0 = (long long)blockIdx.x * chunk + threadIdx.x;
   // The scale needs only the binade of max |v| (truncating the mantissa keeps
   // it) and the centring mean only an estimate (the same value is added back
   // after the product), so both run in FP32 on truncated values.
   float mf = 0.0f, sf = 0.0f;
-  for (int j0 = 0; j0 < kChunk / kT; j0 += kBatch) {
+  for (int j0 = 0; j0 < chunk / kT; j0 += kBatch) {
     double v[kBatch];  // a batch of independent loads in flight per thread
 #pragma unroll
     for (int u = 0; u < kBatch; ++u)
@@ -214,12 +221,12 @@ __global__ void k_split_chunks(const double *__restrict__ src, long long ld_src,
                                long long ncol, const float *__restrict__ colscale,
                                const float *__restrict__ rowscale,
                                const double *__restrict__ rowmean, __half *__restrict__ hi,
-                               __half *__restrict__ lo, long long ld_dst) {
+                               __half *__restrict__ lo, long long ld_dst, int chunk) {
   const long long r = blockIdx.y;
-  const long long c0 = (long long)blockIdx.x * kChunk + threadIdx.x;
+  const long long c0 = (long long)blockIdx.x * chunk + threadIdx.x;
   const double inv = 1.0 / (double)rowscale[r];  // a power of two: exact
   const double shift = rowmean ? -rowmean[r] * inv : 0.0;
-  for (int j0 = 0; j0 < kChunk / kT; j0 += kBatch) {
+  for (int j0 = 0; j0 < chunk / kT; j0 += kBatch) {
     double v[kBatch];
 #pragma unroll
     for (int u = 0; u < kBatch; ++u)
@@ -352,10 +359,12 @@ __global__ void k_splitk_reduce(const float *__restrict__ P, int nsplit, long lo
 
 // The same over groups of four consecutive rows (nrow, ldp and slice
 // multiples of 4, P 16-byte aligned); grid (row blocks, models), no index
-// division.  A thread takes kGroups groups kT quads apart within one model --
-// consecutive threads read consecutive float4s -- and two splits at a time, so
+// division.  A thread takes G groups kT quads apart within one model --
+// consecutive threads read consecutive float4s -- and U splits at a time, so
 // that eight independent 16-byte loads are in flight per thread whatever the
-// number of splits.  The split sums accumulate as unevaluated FP32 pairs
+// number of splits (G = 4 quads x 2 splits for a few splits, 1 quad x 8
+// splits for many, with the next batch loading while one is added up).  The
+// split sums accumulate as unevaluated FP32 pairs
 // (hi + lo, error-free two-sum), about 48 bits -- as good as an FP64 sum of
 // FP32 partials -- without the FP64 pipe.  With more than kPairSplits splits
 // one FP64 add per output widens the pair; with fewer the pair is rounded to
@@ -364,38 +373,54 @@ __global__ void k_splitk_reduce(const float *__restrict__ P, int nsplit, long lo
 // costs as much as the whole memory traffic on this GPU's FP64 pipe.  The
 // power-of-two scales are exponent adds; factor is applied the same way when
 // it is a power of two (fpow2, 2^kfac), else by an FP64 multiply.
-constexpr int kGroups = 4;
 constexpr int kPairSplits = 4;
-template <bool PAIR>  // PAIR: widen hi + lo in FP64 (more than kPairSplits splits)
+// G: row quads per thread (4 for a few splits; 1 for many, so that more
+// threads share the splits' loads); U: splits per load batch.  The next
+// batch of loads is issued before the current one is added up.
+template <bool PAIR, int G>  // PAIR: widen hi + lo in FP64 (more than kPairSplits splits)
 __global__ void __launch_bounds__(kT) k_splitk_reduce4(
     const float *__restrict__ P, int nsplit, long long slice, int nrow, long long ldp,
     const float *__restrict__ rowscale, const float *__restrict__ modscale,
     const double *__restrict__ modmean, const double *__restrict__ rowsum, bool fpow2, int kfac,
     double factor, double *__restrict__ out, long long ld_out) {
+  constexpr int U = G == 1 ? 8 : 2;
   const int nq = nrow / 4;
   const int n = blockIdx.y;
-  const int q0 = blockIdx.x * (kT * kGroups) + threadIdx.x;
+  const int q0 = blockIdx.x * (kT * G) + threadIdx.x;
   const long long s4 = slice / 4;
   const float4 *p = reinterpret_cast<const float4 *>(P + (long long)n * ldp);
-  float hi[kGroups][4], lo[kGroups][4];
+  float hi[G][4], lo[G][4];
 #pragma unroll
-  for (int g = 0; g < kGroups; ++g)
+  for (int g = 0; g < G; ++g)
 #pragma unroll
     for (int i = 0; i < 4; ++i) hi[g][i] = lo[g][i] = 0.0f;
-  for (int s = 0; s < nsplit; s += 2) {
-    float4 q[kGroups][2];
+  float4 q[G][U];
 #pragma unroll
-    for (int g = 0; g < kGroups; ++g)
+  for (int g = 0; g < G; ++g)
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
+    for (int u = 0; u < U; ++u) {
+      const int qi = q0 + g * kT;
+      q[g][u] = (qi < nq && u < nsplit) ? __ldcs(p + (long long)u * s4 + qi)
+                                        : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  for (int s = 0; s < nsplit; s += U) {
+    // many splits: the next batch loads while this one is added up; a few
+    // splits: plain batches (the extra registers cost occupancy)
+    constexpr bool kAhead = G == 1;
+    float4 nx[G][U];
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
         const int qi = q0 + g * kT;
-        q[g][u] = (qi < nq && s + u < nsplit) ? __ldcs(p + (long long)(s + u) * s4 + qi)
-                                              : make_float4(0.f, 0.f, 0.f, 0.f);
+        nx[g][u] = (kAhead && qi < nq && s + U + u < nsplit)
+                       ? __ldcs(p + (long long)(s + U + u) * s4 + qi)
+                       : make_float4(0.f, 0.f, 0.f, 0.f);
       }
 #pragma unroll
-    for (int g = 0; g < kGroups; ++g)
+    for (int g = 0; g < G; ++g)
 #pragma unroll
-      for (int u = 0; u < 2; ++u) {
+      for (int u = 0; u < U; ++u) {
         if (s + u >= nsplit) continue;
         const float x[4] = {q[g][u].x, q[g][u].y, q[g][u].z, q[g][u].w};
 #pragma unroll
@@ -406,10 +431,25 @@ __global__ void __launch_bounds__(kT) k_splitk_reduce4(
           lo[g][i] = __fadd_rn(lo[g][i], err);
         }
       }
+    if (kAhead) {
+#pragma unroll
+      for (int g = 0; g < G; ++g)
+#pragma unroll
+        for (int u = 0; u < U; ++u) q[g][u] = nx[g][u];
+    } else if (s + U < nsplit) {
+#pragma unroll
+      for (int g = 0; g < G; ++g)
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int qi = q0 + g * kT;
+          q[g][u] = (qi < nq && s + U + u < nsplit) ? __ldcs(p + (long long)(s + U + u) * s4 + qi)
+                                                   : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
   }
   const int kmod = (modscale ? pow2_exponent(modscale[n]) : 0) + (fpow2 ? kfac : 0);
 #pragma unroll
-  for (int g = 0; g < kGroups; ++g) {
+  for (int g = 0; g < G; ++g) {
     const int qi = q0 + g * kT;
     if (qi >= nq) continue;
     const int r = qi * 4;
@@ -439,89 +479,125 @@ __global__ void __launch_bounds__(kT) k_splitk_reduce4(
 // Per (station, model): stored-row sums -> raw data (+ background) -> transform.
 // sums [nmod][ld_sums] with row s*NS + q; models [nmod][ld_models] (background
 // values at column ngrid); data [nmod][ld_data]; raw_out [nmod][nmeas*raw] optional.
-__global__ void k_stored_assemble(int kind, int transform, double tbx, double tby, double tbz,
-                                  int nmeas, int nmod, const double *__restrict__ sums,
-                                  long long ld_sums, const double *__restrict__ bgsens, int nbg,
-                                  const double *__restrict__ models, long long ld_models,
-                                  long long ngrid, MagField mf, double *__restrict__ raw_out,
-                                  double *__restrict__ data, long long ld_data) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)nmeas * nmod) return;
-  const int n = t / nmeas, s = t % nmeas;
-  const int raw = kind_raw(kind);
-  const int ns = kind == KIND_MAGNETIC ? 3 : kind_ncomp(kind);
-  const double *sm = sums + n * ld_sums + (long long)s * ns;
-  double r[10];
-  if (kind == KIND_MAGNETIC) {
-    for (int c = 0; c < 3; ++c) r[c] = sm[c];
-  } else {
-    double u[NC_COUNT];
-    for (int c = 0; c < NC_COUNT; ++c) u[c] = 0.0;
-    for (int q = 0; q < ns; ++q) u[slot_comp(kind, q)] = sm[q];
-    raw_from_comps(kind, u, mf, r);
-  }
-  const double *bgval = models + n * ld_models + ngrid;
-  for (int c = 0; c < raw; ++c) {
-    double bg = 0.0;
-    for (int j = 0; j < nbg; ++j)
-      bg = add(bg, mul(bgsens[((long long)s * raw + c) * nbg + j], bgval[j]));
-    r[c] = add(r[c], bg);
-    if (raw_out) raw_out[n * (long long)nmeas * raw + (long long)s * raw + c] = r[c];
-  }
-  double *d = data + n * ld_data;
-  if (transform == TR_NONE) {
-    for (int c = 0; c < raw; ++c) d[(long long)s * raw + c] = r[c];
-  } else if (transform == TR_FTG_INVARIANT) {
-    d[s] = sub(sub(sub(add(add(mul(r[0], r[4]), mul(r[4], r[8])), mul(r[0], r[8])), mul(r[3], r[1])),
-                   mul(r[7], r[5])),
-               mul(r[2], r[6]));
-  } else if (transform == TR_TOTAL_FIELD) {
-    d[s] = sqrt(add(add(mul(r[0], r[0]), mul(r[1], r[1])), mul(r[2], r[2])));
-  } else {
-    d[s] = add(add(mul(tbx, r[0]), mul(tby, r[1])), mul(tbz, r[2]));
-  }
+// KIND is a template argument so that the component arrays stay in
+// registers; one thread per (station, model), a block of kAsm stations of one
+// model (blockIdx.y).  Each station's values are a short record (7 sums, 10
+// raw values), so the block moves its stations' records through shared
+// memory: coalesced reads and writes instead of one strided access per value.
+constexpr int kAsm = 128;
+
+template <int W>
+__device__ __forceinline__ void copy_records(double *dst, const double *src, int count) {
+  for (int i = threadIdx.x; i < count * W; i += blockDim.x) dst[i] = src[i];
 }
 
-// Per (station, model): misfit -> raw weights (through the transform
-// derivative) -> stored-row weights.  w_raw [nmod][nmeas*raw], w_st [nmod][ld_w].
-__global__ void k_stored_weights(int kind, int transform, double tbx, double tby, double tbz,
-                                 int nmeas, int nmod, const double *__restrict__ misfit,
-                                 long long ld_misfit, const double *__restrict__ rawd, MagField mf,
-                                 double *__restrict__ w_raw, double *__restrict__ w_st,
-                                 long long ld_w) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)nmeas * nmod) return;
-  const int n = t / nmeas, s = t % nmeas;
-  const int raw = kind_raw(kind);
-  const int ns = kind == KIND_MAGNETIC ? 3 : kind_ncomp(kind);
-  const double *mis = misfit + n * ld_misfit;
-  double w[10];
-  if (transform == TR_NONE) {
-    for (int c = 0; c < raw; ++c) w[c] = mis[(long long)s * raw + c];
-  } else {
-    const double m = mis[s];
-    const double *d = rawd + n * (long long)nmeas * raw + (long long)s * raw;
-    if (transform == TR_FTG_INVARIANT) {
-      w[0] = mul(m, add(d[4], d[8])); w[1] = mul(m, -d[3]); w[2] = mul(m, -d[6]);
-      w[3] = mul(m, -d[1]); w[4] = mul(m, add(d[0], d[8])); w[5] = mul(m, -d[7]);
-      w[6] = mul(m, -d[2]); w[7] = mul(m, -d[5]); w[8] = mul(m, add(d[0], d[4]));
-    } else if (transform == TR_TOTAL_FIELD) {
-      const double tt = sqrt(add(add(mul(d[0], d[0]), mul(d[1], d[1])), mul(d[2], d[2])));
-      for (int c = 0; c < 3; ++c) w[c] = mul(m, d[c] / tt);
+template <int KIND>
+__global__ void __launch_bounds__(kAsm)
+k_stored_assemble(int transform, double tbx, double tby, double tbz, int nmeas,
+                  const double *__restrict__ sums, long long ld_sums,
+                  const double *__restrict__ bgsens, int nbg, const double *__restrict__ models,
+                  long long ld_models, long long ngrid, MagField mf,
+                  double *__restrict__ raw_out, double *__restrict__ data, long long ld_data) {
+  constexpr int kind = KIND;
+  constexpr int raw = kind_raw(kind);
+  constexpr int ns = kind == KIND_MAGNETIC ? 3 : kind_ncomp(kind);
+  __shared__ double in_rec[kAsm * ns], out_rec[kAsm * raw];
+  const int s0 = blockIdx.x * kAsm, n = blockIdx.y;
+  const int count = min(kAsm, nmeas - s0), t = threadIdx.x, s = s0 + t;
+  copy_records<ns>(in_rec, sums + n * ld_sums + (long long)s0 * ns, count);
+  __syncthreads();
+  double r[10];
+  if (t < count) {
+    const double *sm = in_rec + t * ns;
+    if (kind == KIND_MAGNETIC) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) r[c] = sm[c];
     } else {
-      w[0] = mul(m, tbx); w[1] = mul(m, tby); w[2] = mul(m, tbz);
+      double u[NC_COUNT];
+#pragma unroll
+      for (int c = 0; c < NC_COUNT; ++c) u[c] = 0.0;
+#pragma unroll
+      for (int q = 0; q < ns; ++q) u[slot_comp(kind, q)] = sm[q];
+      raw_from_comps(kind, u, mf, r);
+    }
+    const double *bgval = models + n * ld_models + ngrid;
+#pragma unroll
+    for (int c = 0; c < raw; ++c) {
+      double bg = 0.0;
+      for (int j = 0; j < nbg; ++j)
+        bg = add(bg, mul(bgsens[((long long)s * raw + c) * nbg + j], bgval[j]));
+      r[c] = add(r[c], bg);
+      out_rec[t * raw + c] = r[c];
     }
   }
-  double *wr = w_raw + n * (long long)nmeas * raw + (long long)s * raw;
-  for (int c = 0; c < raw; ++c) wr[c] = w[c];
-  double *ws = w_st + n * ld_w + (long long)s * ns;
-  if (kind == KIND_MAGNETIC) {
-    for (int c = 0; c < 3; ++c) ws[c] = w[c];
-  } else {
-    double u[NC_COUNT];
-    comps_from_raw_weights(kind, w, mf, u);
-    for (int q = 0; q < ns; ++q) ws[q] = u[slot_comp(kind, q)];
+  __syncthreads();
+  if (raw_out)
+    copy_records<raw>(raw_out + n * (long long)nmeas * raw + (long long)s0 * raw, out_rec, count);
+  double *d = data + n * ld_data;
+  if (transform == TR_NONE) {
+    copy_records<raw>(d + (long long)s0 * raw, out_rec, count);
+  } else if (t < count) {
+    if (transform == TR_FTG_INVARIANT) {
+      d[s] = sub(sub(sub(add(add(mul(r[0], r[4]), mul(r[4], r[8])), mul(r[0], r[8])),
+                         mul(r[3], r[1])),
+                     mul(r[7], r[5])),
+                 mul(r[2], r[6]));
+    } else if (transform == TR_TOTAL_FIELD) {
+      d[s] = sqrt(add(add(mul(r[0], r[0]), mul(r[1], r[1])), mul(r[2], r[2])));
+    } else {
+      d[s] = add(add(mul(tbx, r[0]), mul(tby, r[1])), mul(tbz, r[2]));
+    }
   }
+}
+template <int KIND>
+__global__ void __launch_bounds__(kAsm)
+k_stored_weights(int transform, double tbx, double tby, double tbz, int nmeas,
+                 const double *__restrict__ misfit, long long ld_misfit,
+                 const double *__restrict__ rawd, MagField mf, double *__restrict__ w_raw,
+                 double *__restrict__ w_st, long long ld_w) {
+  constexpr int kind = KIND;
+  constexpr int raw = kind_raw(kind);
+  constexpr int ns = kind == KIND_MAGNETIC ? 3 : kind_ncomp(kind);
+  __shared__ double raw_rec[kAsm * raw], st_rec[kAsm * ns];
+  const int s0 = blockIdx.x * kAsm, n = blockIdx.y;
+  const int count = min(kAsm, nmeas - s0), t = threadIdx.x, s = s0 + t;
+  const double *mis = misfit + n * ld_misfit;
+  if (transform == TR_NONE) copy_records<raw>(raw_rec, mis + (long long)s0 * raw, count);
+  __syncthreads();
+  if (t < count) {
+    double w[10];
+    if (transform == TR_NONE) {
+#pragma unroll
+      for (int c = 0; c < raw; ++c) w[c] = raw_rec[t * raw + c];
+    } else {
+      const double m = mis[s];
+      const double *d = rawd + n * (long long)nmeas * raw + (long long)s * raw;
+      if (transform == TR_FTG_INVARIANT) {
+        w[0] = mul(m, add(d[4], d[8])); w[1] = mul(m, -d[3]); w[2] = mul(m, -d[6]);
+        w[3] = mul(m, -d[1]); w[4] = mul(m, add(d[0], d[8])); w[5] = mul(m, -d[7]);
+        w[6] = mul(m, -d[2]); w[7] = mul(m, -d[5]); w[8] = mul(m, add(d[0], d[4]));
+      } else if (transform == TR_TOTAL_FIELD) {
+        const double tt = sqrt(add(add(mul(d[0], d[0]), mul(d[1], d[1])), mul(d[2], d[2])));
+        for (int c = 0; c < 3; ++c) w[c] = mul(m, d[c] / tt);
+      } else {
+        w[0] = mul(m, tbx); w[1] = mul(m, tby); w[2] = mul(m, tbz);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < raw; ++c) raw_rec[t * raw + c] = w[c];
+    if (kind == KIND_MAGNETIC) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) st_rec[t * ns + c] = w[c];
+    } else {
+      double u[NC_COUNT];
+      comps_from_raw_weights(kind, w, mf, u);
+#pragma unroll
+      for (int q = 0; q < ns; ++q) st_rec[t * ns + q] = u[slot_comp(kind, q)];
+    }
+  }
+  __syncthreads();
+  copy_records<raw>(w_raw + n * (long long)nmeas * raw + (long long)s0 * raw, raw_rec, count);
+  copy_records<ns>(w_st + n * ld_w + (long long)s0 * ns, st_rec, count);
 }
 
 // grads[n][ngrid + j] = 2 sum_s sum_r w_raw[n][s][r] bgsens[s][r][j]; block (j, n)
@@ -565,7 +641,8 @@ cudaError_t launch_transpose16(const void *in, long long ld_in, long long rows, 
 }
 
 long long split_matrix_work(int nrow_pad, long long ld_dst) {
-  return 2LL * nrow_pad * ((ld_dst + kChunk - 1) / kChunk);
+  const long long chunk = split_chunk(nrow_pad, ld_dst);
+  return 2LL * nrow_pad * ((ld_dst + chunk - 1) / chunk);
 }
 
 cudaError_t launch_split_matrix(const double *src, long long ld_src, int nrow, long long ncol,
@@ -573,10 +650,11 @@ cudaError_t launch_split_matrix(const double *src, long long ld_src, int nrow, l
                                 int nrow_pad, float *rowscale, double *rowmean, double *work,
                                 cudaStream_t st) {
   if (nrow_pad == 0) return cudaSuccess;
-  const int nchunk = cdiv(ld_dst, kChunk);
+  const int chunk = (int)split_chunk(nrow_pad, ld_dst);
+  const int nchunk = cdiv(ld_dst, chunk);
   double *pmax = work, *psum = work + (long long)nrow_pad * nchunk;
   dim3 grid(nchunk, nrow_pad);
-  k_row_stats<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, pmax, psum, nchunk);
+  k_row_stats<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, pmax, psum, nchunk, chunk);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_row_finalize<<<cdiv(nrow_pad, 128), 128, 0, st>>>(nrow_pad, nchunk, ncol, rowmean != nullptr,
@@ -585,7 +663,7 @@ cudaError_t launch_split_matrix(const double *src, long long ld_src, int nrow, l
   if (e != cudaSuccess) return e;
   k_split_chunks<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, rowscale, rowmean,
                                       static_cast<__half *>(hi), static_cast<__half *>(lo),
-                                      ld_dst);
+                                      ld_dst, chunk);
   return cudaGetLastError();
 }
 
@@ -626,15 +704,17 @@ cudaError_t launch_splitk_reduce(const float *P, int nsplit, long long slice, in
       (reinterpret_cast<uintptr_t>(P) & 15) == 0) {
     int kf = 0;
     const bool fpow2 = factor != 0.0 && std::frexp(factor, &kf) == 0.5;  // factor = 2^(kf-1)
-    dim3 grid(cdiv(nrow / 4, (long long)kT * kGroups), nmod);
-    if (nsplit > kPairSplits)
-      k_splitk_reduce4<true><<<grid, kT, 0, st>>>(P, nsplit, slice, nrow, ldp, rowscale, modscale,
-                                                  modmean, rowsum, fpow2, kf - 1, factor, out,
-                                                  ld_out);
-    else
-      k_splitk_reduce4<false><<<grid, kT, 0, st>>>(P, nsplit, slice, nrow, ldp, rowscale,
-                                                   modscale, modmean, rowsum, fpow2, kf - 1,
-                                                   factor, out, ld_out);
+    if (nsplit > kPairSplits) {  // many splits: one quad per thread, 8 splits per batch
+      dim3 grid(cdiv(nrow / 4, (long long)kT), nmod);
+      k_splitk_reduce4<true, 1><<<grid, kT, 0, st>>>(P, nsplit, slice, nrow, ldp, rowscale,
+                                                     modscale, modmean, rowsum, fpow2, kf - 1,
+                                                     factor, out, ld_out);
+    } else {
+      dim3 grid(cdiv(nrow / 4, (long long)kT * 4), nmod);
+      k_splitk_reduce4<false, 4><<<grid, kT, 0, st>>>(P, nsplit, slice, nrow, ldp, rowscale,
+                                                      modscale, modmean, rowsum, fpow2, kf - 1,
+                                                      factor, out, ld_out);
+    }
     return cudaGetLastError();
   }
   k_splitk_reduce<<<cdiv(n, kT), kT, 0, st>>>(P, nsplit, slice, nmod, nrow, ldp, rowscale,
@@ -648,11 +728,20 @@ cudaError_t launch_stored_assemble(int kind, int transform, double tbx, double t
                                    long long ld_models, long long ngrid, const MagField &mf,
                                    double *raw_out, double *data, long long ld_data,
                                    cudaStream_t st) {
-  const long long n = (long long)nmeas * nmod;
-  if (n == 0) return cudaSuccess;
-  k_stored_assemble<<<cdiv(n, 128), 128, 0, st>>>(kind, transform, tbx, tby, tbz, nmeas, nmod,
-                                                  sums, ld_sums, bgsens, nbg, models, ld_models,
-                                                  ngrid, mf, raw_out, data, ld_data);
+  if ((long long)nmeas * nmod == 0) return cudaSuccess;
+  const dim3 grid(cdiv(nmeas, kAsm), nmod);
+#define J3G_ASSEMBLE(K)                                                                       \
+  k_stored_assemble<K><<<grid, kAsm, 0, st>>>(transform, tbx, tby, tbz, nmeas, sums, ld_sums,  \
+                                             bgsens, nbg, models, ld_models, ngrid, mf,        \
+                                             raw_out, data, ld_data)
+  switch (kind) {
+    case KIND_SCALAR: J3G_ASSEMBLE(KIND_SCALAR); break;
+    case KIND_TENSOR: J3G_ASSEMBLE(KIND_TENSOR); break;
+    case KIND_MAGNETIC: J3G_ASSEMBLE(KIND_MAGNETIC); break;
+    case KIND_JOINT: J3G_ASSEMBLE(KIND_JOINT); break;
+    default: return cudaErrorInvalidValue;
+  }
+#undef J3G_ASSEMBLE
   return cudaGetLastError();
 }
 
@@ -660,10 +749,19 @@ cudaError_t launch_stored_weights(int kind, int transform, double tbx, double tb
                                   int nmeas, int nmod, const double *misfit, long long ld_misfit,
                                   const double *rawd, const MagField &mf, double *w_raw,
                                   double *w_st, long long ld_w, cudaStream_t st) {
-  const long long n = (long long)nmeas * nmod;
-  if (n == 0) return cudaSuccess;
-  k_stored_weights<<<cdiv(n, 128), 128, 0, st>>>(kind, transform, tbx, tby, tbz, nmeas, nmod,
-                                                 misfit, ld_misfit, rawd, mf, w_raw, w_st, ld_w);
+  if ((long long)nmeas * nmod == 0) return cudaSuccess;
+  const dim3 grid(cdiv(nmeas, kAsm), nmod);
+#define J3G_WEIGHTS(K)                                                                         \
+  k_stored_weights<K><<<grid, kAsm, 0, st>>>(transform, tbx, tby, tbz, nmeas, misfit, ld_misfit, \
+                                            rawd, mf, w_raw, w_st, ld_w)
+  switch (kind) {
+    case KIND_SCALAR: J3G_WEIGHTS(KIND_SCALAR); break;
+    case KIND_TENSOR: J3G_WEIGHTS(KIND_TENSOR); break;
+    case KIND_MAGNETIC: J3G_WEIGHTS(KIND_MAGNETIC); break;
+    case KIND_JOINT: J3G_WEIGHTS(KIND_JOINT); break;
+    default: return cudaErrorInvalidValue;
+  }
+#undef J3G_WEIGHTS
   return cudaGetLastError();
 }
 
