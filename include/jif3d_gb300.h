@@ -343,6 +343,12 @@ int j3g_get_timing(j3g_context *ctx, int category, double *total_ms, long long *
  * made while the stream is being captured into a CUDA graph; results can
  * differ from the fixed plan's in the last bits (another summation order). */
 int j3g_set_autotune(j3g_context *ctx, int enable);
+/* Fix the plan of one direction (0 forward, 1 adjoint): K splits and N tile
+ * (0 = by the number of models, 64, 128, 256; a tile the batch does not fill
+ * falls back to the automatic plan).  nsplit <= 0 returns to the fixed rule or
+ * the autotuner.  For reproducible runs with a plan found by tuning; more
+ * than 64 k-blocks per split loses accuracy (the split sums are FP32). */
+int j3g_set_gemm_plan(j3g_context *ctx, int direction, int nsplit, int tile);
 /* The plan the last batched product used: direction 0 forward (J M), 1
  * adjoint (J^T R); K splits requested, N tile (64, 128 or 256 = CTA pair) and
  * the autotuner's time of that plan in ms (0 for the fixed rule). */

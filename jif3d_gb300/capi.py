@@ -67,6 +67,7 @@ SIGNATURES = {
     "j3g_subsets_lqderivative_device": (_I, [_VP, _I, ctypes.POINTER(_I), ctypes.POINTER(_I),
                                              _VP, _VP, _VP]),
     "j3g_set_autotune": (_I, [_VP, _I]),
+    "j3g_set_gemm_plan": (_I, [_VP, _I, _I, _I]),
     "j3g_get_gemm_plan": (_I, [_VP, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), _P]),
     "j3g_refine_axis": (_I, [_I, _P, _P, _I, _P, _I, _P, ctypes.POINTER(_I)]),
     "j3g_set_refinement": (_I, [_VP, _I, _I, _I, _P, _P, _P]),
@@ -552,6 +553,10 @@ class Context:
 
     def set_autotune(self, enable=True):
         self._check(self._lib.j3g_set_autotune(self._h, 1 if enable else 0))
+
+    def set_gemm_plan(self, direction, nsplit, tile=0):
+        """Pin the plan of a direction; nsplit <= 0 unpins it."""
+        self._check(self._lib.j3g_set_gemm_plan(self._h, int(direction), int(nsplit), int(tile)))
 
     def gemm_plan(self, direction):
         ns, tile, ms = _I(), _I(), _D()

@@ -80,6 +80,8 @@ struct j3g_context {
     float ms = 0.0f;  // timed by the autotuner (0 for the fixed rule)
   };
   bool autotune = false;
+  bool pinned[2] = {false, false};  // plans fixed by j3g_set_gemm_plan, per direction
+  GemmPlan pinned_plan[2];
 
   // station subsets (j3g_subsets_*): a context over the concatenated subset
   // stations, rebuilt when the subsets or this context's setup change
@@ -712,6 +714,15 @@ int gemm_plan(j3g_context *c, int dir, const GemmOperands &g, long long ldp, lon
   plan.tile = tile0;
   plan.nsplit = choose_splits(g.m, (int)(g.n_pad / tile0), g.ld);
   plan.ms = 0.0f;
+  if (c->pinned[dir]) {
+    const auto &pp = c->pinned_plan[dir];
+    if (pp.tile == 0 || g.n_pad % pp.tile == 0) {  // a tile that fits the batch
+      plan.nsplit = pp.nsplit;
+      if (pp.tile) plan.tile = pp.tile;
+      return ensure(c, c->P,
+                    sizeof(float) * (size_t)gemm_splits_used(g.ld, plan.nsplit) * slice);
+    }
+  }
   const std::array<long long, 4> key{dir, g.m, g.n_pad, g.ld};
   auto it = c->autotune ? c->plans.find(key) : c->plans.end();
   if (!c->autotune || it != c->plans.end()) {
@@ -747,6 +758,7 @@ int gemm_plan(j3g_context *c, int dir, const GemmOperands &g, long long ldp, lon
   }
   int nsp_max = 1;
   for (auto &p : cand) nsp_max = std::max(nsp_max, gemm_splits_used(g.ld, p.second));
+
   J3G_TRY(ensure(c, c->P, sizeof(float) * (size_t)nsp_max * slice));
   float *P = ptr<float>(c->P);
   cudaEvent_t a, b;
@@ -1530,6 +1542,21 @@ int j3g_subsets_lqderivative_device(j3g_context *c, int nsub, const int *h_offse
 int j3g_set_autotune(j3g_context *c, int enable) {
   if (!c) return J3G_ERR_ARG;
   c->autotune = enable != 0;
+  return J3G_OK;
+}
+
+int j3g_set_gemm_plan(j3g_context *c, int direction, int nsplit, int tile) {
+  if (!c || direction < 0 || direction > 1) return J3G_ERR_ARG;
+  if (nsplit <= 0) {  // back to the fixed rule / the autotuner
+    c->pinned[direction] = false;
+    return J3G_OK;
+  }
+  if (tile != 0 && tile != 64 && tile != 128 && tile != 256)
+    return fail(c, J3G_ERR_ARG, "tile must be 0, 64, 128 or 256");
+  c->pinned[direction] = true;
+  c->pinned_plan[direction].nsplit = nsplit;
+  c->pinned_plan[direction].tile = tile;
+  c->pinned_plan[direction].ms = 0.0f;
   return J3G_OK;
 }
 

@@ -171,6 +171,40 @@ def test_pipelined_batched_calls(ctx, kind, transform):
         ctx.batched_wait(10 ** 9)
 
 
+def test_pinned_gemm_plans(ctx, oracle_lib):
+    """Pinned plans (j3g_set_gemm_plan) are used as given -- the CTA pair with
+    many K splits, one-SM 128-wide tiles -- and agree with the oracle; a tile
+    the batch does not fill falls back to the automatic plan; unpinning
+    restores the fixed rule."""
+    s = small_survey(W.JOINT, seed=290, nx=16, ny=14, nz=10, nmeas=40)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    rng = np.random.default_rng(29)
+    models = s.model[None, :] + 2.0 * rng.normal(size=(300, s.nparm))
+    mis = rng.normal(size=(300, s.stations.shape[0] * 10))
+    try:
+        for plan_f, plan_a in (((50, 256), (5, 256)), ((8, 128), (3, 128))):
+            ctx.set_gemm_plan(0, *plan_f)
+            ctx.set_gemm_plan(1, *plan_a)
+            d = ctx.batched_forward(models)
+            g = ctx.batched_lqderivative(models, mis)
+            assert ctx.gemm_plan(0) == dict(nsplit=plan_f[0], tile=plan_f[1], tuned_ms=0.0)
+            assert ctx.gemm_plan(1) == dict(nsplit=plan_a[0], tile=plan_a[1], tuned_ms=0.0)
+            for i in (0, 299):
+                check_groups(s, d[i], oracle_forward(oracle_lib, s, models[i]))
+                assert relerr(g[i], oracle_lqderivative(oracle_lib, s, mis[i], models[i])) <= TOL
+        ctx.set_gemm_plan(0, 4, 256)
+        ctx.batched_forward(models[:10])  # 10 models: the 256 tile does not fit
+        assert ctx.gemm_plan(0)["tile"] == 64
+    finally:
+        ctx.set_gemm_plan(0, 0)
+        ctx.set_gemm_plan(1, 0)
+    ctx.batched_forward(models)
+    assert ctx.gemm_plan(0)["nsplit"] != 50
+    with pytest.raises(capi.J3GError):
+        ctx.set_gemm_plan(0, 4, 96)
+
+
 def test_stored_is_dropped_on_new_geometry(ctx):
     s = small_survey(W.SCALAR, seed=5)
     W.setup_context(ctx, s)
