@@ -311,6 +311,8 @@ int gridded_node_forward(j3g_context *c, const double *d_model) {
   };
   while (npb > 256 && blocks(npb, spb) < kTargetBlocks) npb >>= 1;
   while (spb > 1 && blocks(npb, spb) < kTargetBlocks) spb >>= 1;
+  // station blocks run over grid y: at most 65535 of them
+  spb = std::max(spb, (c->nmeas + 65534) / 65535);
   const int nblk = (int)((nn + npb - 1) / npb);
   const int ncomp = kind_ncomp(c->kind);
   J3G_TRY(ensure(c, c->partial, sizeof(double) * (size_t)nblk * c->nmeas * ncomp));
@@ -794,7 +796,12 @@ int gemm_plan(j3g_context *c, int dir, const GemmOperands &g, long long ldp, lon
   return J3G_OK;
 }
 
-int batched_forward_impl(j3g_context *c, int nmod, const double *d_models, double *d_data,
+// Models per pass of the batched products: the model index of the split,
+// reduction and epilogue kernels runs over grid y (at most 65535 blocks) and
+// the product pads the batch to a multiple of 256.
+constexpr int kMaxBatch = 32768;
+
+int batched_forward_pass(j3g_context *c, int nmod, const double *d_models, double *d_data,
                          double *raw_out) {
   const long long K = c->ngrid(), ldK = c->st_ld, R = c->st_rows, np = c->nparm();
   double tbx, tby, tbz;
@@ -852,7 +859,17 @@ int batched_forward_impl(j3g_context *c, int nmod, const double *d_models, doubl
   return J3G_OK;
 }
 
-int batched_adjoint_impl(j3g_context *c, int nmod, const double *d_models,
+// Batches of more than kMaxBatch models run as consecutive passes.
+int batched_forward_impl(j3g_context *c, int nmod, const double *d_models, double *d_data,
+                         double *raw_out) {
+  const size_t np = c->nparm(), nd = (size_t)c->nmeas * c->dpm(), nr = (size_t)c->nmeas * c->raw();
+  for (int n0 = 0; n0 < nmod; n0 += kMaxBatch)
+    J3G_TRY(batched_forward_pass(c, std::min(kMaxBatch, nmod - n0), d_models + n0 * np,
+                                 d_data + n0 * nd, raw_out ? raw_out + n0 * nr : nullptr));
+  return J3G_OK;
+}
+
+int batched_adjoint_pass(j3g_context *c, int nmod, const double *d_models,
                          const double *d_misfits, double *d_grads) {
   const long long K = c->ngrid(), ldK = c->st_ld, R = c->st_rows, ldR = c->st_ldT,
                   np = c->nparm();
@@ -863,7 +880,7 @@ int batched_adjoint_impl(j3g_context *c, int nmod, const double *d_models,
   if (c->transform == J3G_T_FTG_INVARIANT || c->transform == J3G_T_TOTAL_FIELD) {
     J3G_TRY(ensure(c, c->rawb, sizeof(double) * (size_t)nmod * c->nmeas * raw));
     J3G_TRY(ensure(c, c->data, sizeof(double) * (size_t)nmod * c->nmeas * c->dpm()));
-    J3G_TRY(batched_forward_impl(c, nmod, d_models, ptr<double>(c->data), ptr<double>(c->rawb)));
+    J3G_TRY(batched_forward_pass(c, nmod, d_models, ptr<double>(c->data), ptr<double>(c->rawb)));
     rawd = ptr<double>(c->rawb);
   }
   J3G_TRY(ensure(c, c->wrawb, sizeof(double) * (size_t)nmod * c->nmeas * raw));
@@ -920,6 +937,16 @@ int batched_adjoint_impl(j3g_context *c, int nmod, const double *d_models,
     J3G_LAUNCH(c, launch_bg_grad_batched(raw, c->nmeas, nbg, nmod, ptr<double>(c->wrawb),
                                          ptr<double>(c->bgsens), d_grads, np, K, c->stream));
   }
+  return J3G_OK;
+}
+
+int batched_adjoint_impl(j3g_context *c, int nmod, const double *d_models,
+                         const double *d_misfits, double *d_grads) {
+  const size_t np = c->nparm(), nd = (size_t)c->nmeas * c->dpm();
+  for (int n0 = 0; n0 < nmod; n0 += kMaxBatch)
+    J3G_TRY(batched_adjoint_pass(c, std::min(kMaxBatch, nmod - n0),
+                                 d_models ? d_models + n0 * np : nullptr, d_misfits + n0 * nd,
+                                 d_grads + n0 * np));
   return J3G_OK;
 }
 

@@ -199,8 +199,8 @@ template <int BN, bool F16>
 __global__ void __launch_bounds__(kGemmThreads, 1)
     k_gemm_x3(const __grid_constant__ CUtensorMap tmAhi, const __grid_constant__ CUtensorMap tmAlo,
               const __grid_constant__ CUtensorMap tmBhi, const __grid_constant__ CUtensorMap tmBlo,
-              int kb_per_split, int kb_total, int M, int N, float *__restrict__ P, long long ldp,
-              long long slice, int *__restrict__ err) {
+              int kb_per_split, int kb_total, int M, int N, int ntn, float *__restrict__ P,
+              long long ldp, long long slice, int *__restrict__ err) {
   using C = Cfg<BN, F16>;
   constexpr int S = C::STAGES;
   extern __shared__ uint8_t smem_raw[];
@@ -212,7 +212,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + C::NBAR);
   volatile int *fail = reinterpret_cast<volatile int *>(tmem_slot + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;  // N tiles fastest (see launch_bn)
+  // x runs over (M tile, N tile) with the ntn N tiles fastest (see launch_bn)
+  const int n0 = (int)(blockIdx.x % ntn) * BN, m0 = (int)(blockIdx.x / ntn) * BM;
   const int kb0 = blockIdx.z * kb_per_split;
   const int nkb = min(kb_total, kb0 + kb_per_split) - kb0;
   const int ndrain = nkb * kDrainsPerBlock;
@@ -780,10 +781,13 @@ cudaError_t launch_bn(const GemmOperands &g, int nsplit, float *P, long long ldp
   cudaError_t e = allow_smem_once(reinterpret_cast<const void *>(k_gemm_x3<BN, F16>),
                                   Cfg<BN, F16>::SMEM);
   if (e != cudaSuccess) return e;
-  // N tiles vary fastest so the CTAs sharing an A tile run side by side (L2 reuse)
-  dim3 grid((unsigned)(g.n_pad / BN), (unsigned)((g.m + BM - 1) / BM), (unsigned)nsp);
+  // N tiles vary fastest so the CTAs sharing an A tile run side by side (L2
+  // reuse); M and N tiles share grid x, whose limit (2^31 - 1) no mesh reaches
+  const int ntn = (int)(g.n_pad / BN);
+  const long long nmt = (g.m + BM - 1) / BM;
+  dim3 grid((unsigned)(nmt * ntn), 1u, (unsigned)nsp);
   k_gemm_x3<BN, F16><<<grid, kGemmThreads, Cfg<BN, F16>::SMEM, st>>>(
-      ah, al, bh, bl, kb_per, kb_total, (int)g.m, (int)g.n, P, ldp, slice, err);
+      ah, al, bh, bl, kb_per, kb_total, (int)g.m, (int)g.n, ntn, P, ldp, slice, err);
   return cudaGetLastError();
 }
 

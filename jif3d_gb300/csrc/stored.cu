@@ -17,6 +17,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
@@ -124,16 +125,20 @@ __global__ void k_split_rows(const double *__restrict__ rows, long long ld_in, l
 __global__ void k_transpose16(const uint16_t *__restrict__ in, long long ld_in, long long rows,
                               long long cols, uint16_t *__restrict__ out, long long ld_out) {
   __shared__ uint16_t tile[32][34];
-  const long long c0 = (long long)blockIdx.x * 32, r0 = (long long)blockIdx.y * 32;
+  const long long c0 = (long long)blockIdx.x * 32;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
-  for (int k = ty; k < 32; k += 8) {
-    const long long r = r0 + k, c = c0 + tx;
-    tile[k][tx] = (r < rows && c < cols) ? in[tiled_index(r, c, ld_in)] : (uint16_t)0;
-  }
-  __syncthreads();
-  for (int k = ty; k < 32; k += 8) {
-    const long long c = c0 + k, r = r0 + tx;
-    if (c < cols && r < ld_out) out[tiled_index(c, r, ld_out)] = tile[tx][k];
+  // row blocks loop over grid y (at most 65535 blocks)
+  for (long long r0 = (long long)blockIdx.y * 32; r0 < ld_out; r0 += (long long)gridDim.y * 32) {
+    __syncthreads();  // the previous block's tile has been written out
+    for (int k = ty; k < 32; k += 8) {
+      const long long r = r0 + k, c = c0 + tx;
+      tile[k][tx] = (r < rows && c < cols) ? in[tiled_index(r, c, ld_in)] : (uint16_t)0;
+    }
+    __syncthreads();
+    for (int k = ty; k < 32; k += 8) {
+      const long long c = c0 + k, r = r0 + tx;
+      if (c < cols && r < ld_out) out[tiled_index(c, r, ld_out)] = tile[tx][k];
+    }
   }
 }
 
@@ -292,31 +297,35 @@ __global__ void __launch_bounds__(kT) k_gemv_t_f32(const float *__restrict__ J, 
                                                    int nrows, const double *__restrict__ w,
                                                    double *__restrict__ part) {
   const long long c4 = (long long)blockIdx.x * kT + threadIdx.x;  // float4 column index
-  const int chunk = blockIdx.y;
-  const int r0 = chunk * kRC, r1 = min(nrows, r0 + kRC);
+  const int nchunk = (nrows + kRC - 1) / kRC;
   __shared__ float ws[kRC];
-  for (int t = threadIdx.x; t < kRC; t += kT) ws[t] = (r0 + t < r1) ? (float)w[r0 + t] : 0.0f;
-  __syncthreads();
-  if (c4 * 4 >= ld) return;
-  double d0 = 0, d1 = 0, d2 = 0, d3 = 0;
-  float f0 = 0, f1 = 0, f2 = 0, f3 = 0;
-  int cnt = 0;
-  for (int r = r0; r < r1; ++r) {
-    const float4 a = __ldcs(reinterpret_cast<const float4 *>(J + (long long)r * ld) + c4);
-    const float wr = ws[r - r0];
-    f0 = fmaf(a.x, wr, f0);
-    f1 = fmaf(a.y, wr, f1);
-    f2 = fmaf(a.z, wr, f2);
-    f3 = fmaf(a.w, wr, f3);
-    if (++cnt == 16) {
-      d0 += f0; d1 += f1; d2 += f2; d3 += f3;
-      f0 = f1 = f2 = f3 = 0.0f;
-      cnt = 0;
+  // row chunks loop over grid y (at most 65535 blocks)
+  for (int chunk = blockIdx.y; chunk < nchunk; chunk += gridDim.y) {
+    const int r0 = chunk * kRC, r1 = min(nrows, r0 + kRC);
+    __syncthreads();  // the previous chunk's weights are no longer read
+    for (int t = threadIdx.x; t < kRC; t += kT) ws[t] = (r0 + t < r1) ? (float)w[r0 + t] : 0.0f;
+    __syncthreads();
+    if (c4 * 4 >= ld) continue;
+    double d0 = 0, d1 = 0, d2 = 0, d3 = 0;
+    float f0 = 0, f1 = 0, f2 = 0, f3 = 0;
+    int cnt = 0;
+    for (int r = r0; r < r1; ++r) {
+      const float4 a = __ldcs(reinterpret_cast<const float4 *>(J + (long long)r * ld) + c4);
+      const float wr = ws[r - r0];
+      f0 = fmaf(a.x, wr, f0);
+      f1 = fmaf(a.y, wr, f1);
+      f2 = fmaf(a.z, wr, f2);
+      f3 = fmaf(a.w, wr, f3);
+      if (++cnt == 16) {
+        d0 += f0; d1 += f1; d2 += f2; d3 += f3;
+        f0 = f1 = f2 = f3 = 0.0f;
+        cnt = 0;
+      }
     }
+    d0 += f0; d1 += f1; d2 += f2; d3 += f3;
+    double *o = part + (long long)chunk * ld + c4 * 4;
+    o[0] = d0; o[1] = d1; o[2] = d2; o[3] = d3;
   }
-  d0 += f0; d1 += f1; d2 += f2; d3 += f3;
-  double *o = part + (long long)chunk * ld + c4 * 4;
-  o[0] = d0; o[1] = d1; o[2] = d2; o[3] = d3;
 }
 
 __global__ void k_sum_parts(const double *__restrict__ part, int nchunk, long long ld,
@@ -634,7 +643,7 @@ cudaError_t launch_split_rows(const double *rows, long long ld_in, long long nco
 
 cudaError_t launch_transpose16(const void *in, long long ld_in, long long rows, long long cols,
                                void *out, long long ld_out, cudaStream_t st) {
-  dim3 grid(cdiv(cols, 32), cdiv(ld_out, 32));
+  dim3 grid(cdiv(cols, 32), std::min(cdiv(ld_out, 32), 65535));
   k_transpose16<<<grid, 256, 0, st>>>(static_cast<const uint16_t *>(in), ld_in, rows, cols,
                                       static_cast<uint16_t *>(out), ld_out);
   return cudaGetLastError();
@@ -686,7 +695,7 @@ cudaError_t launch_gemv_t_f32(const float *J, long long ld, int nrows, const dou
                               double *part, long long ncol, double factor, double *out,
                               cudaStream_t st) {
   const int nchunk = gemv_t_chunks(nrows);
-  dim3 grid(cdiv(ld / 4, kT), nchunk);
+  dim3 grid(cdiv(ld / 4, kT), std::min(nchunk, 65535));
   k_gemv_t_f32<<<grid, kT, 0, st>>>(J, ld, nrows, w, part);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
