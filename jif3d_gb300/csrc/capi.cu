@@ -131,6 +131,9 @@ struct j3g_context {
   // background layers that respond (none for the vertical gradient and
   // magnetisation: OMPMagneticGradImp.h:32-40, OMPMagnetizationImp.cpp:16-22)
   int nbg_active() const { return kind_special(kind) ? 0 : (int)bg.size(); }
+  // background parameters of a model; those of the vertical gradient have
+  // no response, so their gradient entries are zero
+  int nbg_params() const { return (int)(nparm() - ngrid_cols()); }
   long long nnodes() const { return (long long)(nx + 1) * (ny + 1) * (nz + 1); }
   int raw() const { return kind_raw(kind); }
   int dpm() const { return transform == J3G_T_NONE ? raw() : 1; }
@@ -557,16 +560,13 @@ int build_stored(j3g_context *c, int storage) {
   J3G_TRY(check_ready(c));
   if (storage != J3G_STORE_FP32 && storage != J3G_STORE_F16X2)
     return fail(c, J3G_ERR_ARG, "unknown storage");
-  if (kind_special(c->kind))
-    return fail(c, J3G_ERR_UNSUPPORTED,
-                "device sensitivity is built for gravity, FTG and induced magnetics only");
   if (!c->node_exact)
     return fail(c, J3G_ERR_UNSUPPORTED,
                 "device sensitivity needs corner coordinates that are running sums of the sizes");
   if (c->ngrid() == 0 || c->nmeas == 0) return fail(c, J3G_ERR_ARG, "empty mesh or survey");
   drop_stored(c);
   J3G_TRY(ensure_background(c));
-  const long long K = c->ngrid(), ldK = round64(K);
+  const long long K = c->ngrid_cols(), ldK = round64(K);
   const int NS = nstored(c);
   const long long R = (long long)c->nmeas * NS, ldR = round64(R);
   const size_t need = storage == J3G_STORE_FP32
@@ -641,7 +641,7 @@ int batched_forward_impl(j3g_context *c, int nmod, const double *d_models, doubl
 
 // d = J m through the FP32 streaming product (one model), then background + transform.
 int stored_forward_f32(j3g_context *c, const double *d_model, double *d_data, double *raw_out) {
-  const long long K = c->ngrid(), ldK = c->st_ld, R = c->st_rows;
+  const long long K = c->ngrid_cols(), ldK = c->st_ld, R = c->st_rows;
   double tbx, tby, tbz;
   tfa_dir(c, tbx, tby, tbz);
   J3G_TRY(ensure(c, c->x32, sizeof(float) * (size_t)ldK));
@@ -652,7 +652,7 @@ int stored_forward_f32(j3g_context *c, const double *d_model, double *d_data, do
     J3G_LAUNCH(c, launch_gemv_f32(ptr<float>(c->J32), ldK, (int)R, ptr<float>(c->x32),
                                   ptr<double>(c->sums), c->stream));
   }
-  const int nbg = (int)c->bg.size();
+  const int nbg = c->nbg_active();
   J3G_LAUNCH(c, launch_stored_assemble(c->kind, c->transform, tbx, tby, tbz, c->nmeas, 1,
                                        ptr<double>(c->sums), R, nbg ? ptr<double>(c->bgsens) : nullptr,
                                        nbg, d_model, c->nparm(), K, mag_field(c), raw_out, d_data,
@@ -660,10 +660,21 @@ int stored_forward_f32(j3g_context *c, const double *d_model, double *d_data, do
   return J3G_OK;
 }
 
+// Gradient entries of background parameters without a response (vertical
+// gradient): zero, for nmod gradients [nmod][nparm].
+int zero_inert_background(j3g_context *c, int nmod, double *d_grads) {
+  const int ninert = c->nbg_params() - c->nbg_active();
+  if (ninert <= 0 || nmod == 0) return J3G_OK;
+  const size_t np = c->nparm();
+  J3G_CUDA(c, cudaMemset2DAsync(d_grads + (np - ninert), np * sizeof(double), 0,
+                                ninert * sizeof(double), nmod, c->stream));
+  return J3G_OK;
+}
+
 int stored_adjoint_f32(j3g_context *c, const double *d_model, const double *d_misfit,
                        double *d_grad) {
-  const long long K = c->ngrid(), ldK = c->st_ld, R = c->st_rows;
-  const int raw = c->raw(), nbg = (int)c->bg.size();
+  const long long K = c->ngrid_cols(), ldK = c->st_ld, R = c->st_rows;
+  const int raw = c->raw(), nbg = c->nbg_active();
   double tbx, tby, tbz;
   tfa_dir(c, tbx, tby, tbz);
   const double *rawd = nullptr;
@@ -688,7 +699,7 @@ int stored_adjoint_f32(j3g_context *c, const double *d_model, const double *d_mi
   if (nbg)
     J3G_LAUNCH(c, launch_bg_grad_batched(raw, c->nmeas, nbg, 1, ptr<double>(c->wrawb),
                                          ptr<double>(c->bgsens), d_grad, c->nparm(), K, c->stream));
-  return J3G_OK;
+  return zero_inert_background(c, 1, d_grad);
 }
 
 // K-splits of a tensor-core product: at most 64 k-blocks (4096 products) per
@@ -803,10 +814,10 @@ constexpr int kMaxBatch = 32768;
 
 int batched_forward_pass(j3g_context *c, int nmod, const double *d_models, double *d_data,
                          double *raw_out) {
-  const long long K = c->ngrid(), ldK = c->st_ld, R = c->st_rows, np = c->nparm();
+  const long long K = c->ngrid_cols(), ldK = c->st_ld, R = c->st_rows, np = c->nparm();
   double tbx, tby, tbz;
   tfa_dir(c, tbx, tby, tbz);
-  const int nbg = (int)c->bg.size();
+  const int nbg = c->nbg_active();
   J3G_TRY(ensure(c, c->sums, sizeof(double) * (size_t)nmod * R));
   if (c->storage == J3G_STORE_FP32) {
     for (int n = 0; n < nmod; ++n) {
@@ -871,9 +882,9 @@ int batched_forward_impl(j3g_context *c, int nmod, const double *d_models, doubl
 
 int batched_adjoint_pass(j3g_context *c, int nmod, const double *d_models,
                          const double *d_misfits, double *d_grads) {
-  const long long K = c->ngrid(), ldK = c->st_ld, R = c->st_rows, ldR = c->st_ldT,
+  const long long K = c->ngrid_cols(), ldK = c->st_ld, R = c->st_rows, ldR = c->st_ldT,
                   np = c->nparm();
-  const int raw = c->raw(), nbg = (int)c->bg.size();
+  const int raw = c->raw(), nbg = c->nbg_active();
   double tbx, tby, tbz;
   tfa_dir(c, tbx, tby, tbz);
   const double *rawd = nullptr;
@@ -937,7 +948,7 @@ int batched_adjoint_pass(j3g_context *c, int nmod, const double *d_models,
     J3G_LAUNCH(c, launch_bg_grad_batched(raw, c->nmeas, nbg, nmod, ptr<double>(c->wrawb),
                                          ptr<double>(c->bgsens), d_grads, np, K, c->stream));
   }
-  return J3G_OK;
+  return zero_inert_background(c, nmod, d_grads);
 }
 
 int batched_adjoint_impl(j3g_context *c, int nmod, const double *d_models,
@@ -1297,11 +1308,11 @@ int j3g_sensitivity_info(const j3g_context *c, int *storage, long long *rows, lo
   if (!c) return J3G_ERR_ARG;
   if (storage) *storage = c->storage;
   if (rows) *rows = c->storage ? c->st_rows : 0;
-  if (cols) *cols = c->storage ? c->ngrid() : 0;
+  if (cols) *cols = c->storage ? c->ngrid_cols() : 0;
   if (bytes)
     *bytes = c->storage == J3G_STORE_FP32     ? c->st_rows * c->st_ld * 4
              : c->storage == J3G_STORE_F16X2 ? 2 * (tiled_rows(c->st_rows) * c->st_ld * 2) +
-                                                   2 * (tiled_rows(c->ngrid()) * c->st_ldT * 2)
+                                                   2 * (tiled_rows(c->ngrid_cols()) * c->st_ldT * 2)
                                               : 0;
   return J3G_OK;
 }

@@ -110,9 +110,19 @@ __host__ __device__ inline int kind_nblock(int kind) {
   return kind == KIND_MAGNETIZATION ? 3 : 1;
 }
 // The node path reduces these kinds to raw rows directly (no node-component
-// layout); they have no background response and no stored-sensitivity path.
-__host__ __device__ inline bool kind_special(int kind) {
+// layout); they have no background response.
+__host__ __device__ constexpr inline bool kind_special(int kind) {
   return kind == KIND_MAG_GRADIENT || kind == KIND_MAGNETIZATION;
+}
+// Rows of the device-resident sensitivity per station: the raw rows for the
+// magnetic kinds (Bx By Bz; the vertical gradient; the three field
+// components over the three magnetisation blocks), else the kind's node
+// components (scalar 1, tensor 6, joint 7), from which the raw rows follow.
+__host__ __device__ constexpr inline bool stored_is_raw(int kind) {
+  return kind == KIND_MAGNETIC || kind_special(kind);
+}
+__host__ __device__ constexpr inline int stored_rows(int kind) {
+  return stored_is_raw(kind) ? kind_raw(kind) : kind_ncomp(kind);
 }
 // Slot s of a kind's compact component list -> node component id.
 __host__ __device__ constexpr inline int slot_comp(int kind, int s) {

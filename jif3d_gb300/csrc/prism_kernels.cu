@@ -463,9 +463,9 @@ __global__ void __launch_bounds__(kThreads)
 // raw_from_vc (BzSensBot - BzSensTop, OMPMagneticGradImp.cpp:88-99) and
 // magnetisation as factor * U_kj in row k, column block j
 // (OMPMagnetizationImp.cpp:58-68, 93-104).
-template <int KIND>
+template <int KIND, class OutT = double>
 __device__ __forceinline__ void store_cell_rows(const double *u, const MagField &mf,
-                                                long long ngrid, long long cell, double *rows,
+                                                long long ngrid, long long cell, OutT *rows,
                                                 long long ld) {
   using T = KindTraits<KIND>;
   if constexpr (KIND == KIND_MAGNETIZATION) {
@@ -473,11 +473,11 @@ __device__ __forceinline__ void store_cell_rows(const double *u, const MagField 
     for (int k = 0; k < 3; ++k)
 #pragma unroll
       for (int jb = 0; jb < 3; ++jb)
-        rows[(long long)k * ld + jb * ngrid + cell] = mul(mf.factor, u[3 * k + jb]);
+        rows[(long long)k * ld + jb * ngrid + cell] = (OutT)mul(mf.factor, u[3 * k + jb]);
   } else if constexpr (KIND == KIND_MAG_GRADIENT) {
     double raw[3];
     raw_from_vc(KIND, u, mf, raw);
-    rows[cell] = raw[0];
+    rows[cell] = (OutT)raw[0];
   } else {
     double c[NC_COUNT];
 #pragma unroll
@@ -485,7 +485,7 @@ __device__ __forceinline__ void store_cell_rows(const double *u, const MagField 
     double raw[10];
     raw_from_comps(KIND, c, mf, raw);
 #pragma unroll
-    for (int r = 0; r < T::raw; ++r) rows[(long long)r * ld + cell] = raw[r];
+    for (int r = 0; r < T::raw; ++r) rows[(long long)r * ld + cell] = (OutT)raw[r];
   }
 }
 
@@ -518,10 +518,12 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // Stored rows for the device-resident sensitivity: the node components of the
-// kind (scalar 1, tensor 6, joint 7) or the 3 raw magnetic rows, one row per
-// (station, stored component), written as OutT (double or float).
+// kind (scalar 1, tensor 6, joint 7) or the raw magnetic rows (3 of Bx By Bz;
+// 1 of the vertical gradient; 3 over the three magnetisation blocks, columns
+// block * ngrid + cell), one row per (station, stored component), written as
+// OutT (double or float).
 template <int KIND> struct StoredRows {
-  static constexpr int n = (KIND == KIND_MAGNETIC) ? 3 : KindTraits<KIND>::ncomp;
+  static constexpr int n = stored_rows(KIND);
 };
 
 template <int KIND, class OutT>
@@ -540,24 +542,39 @@ __global__ void __launch_bounds__(kThreads)
   const int i = t / m.ny;
   const int ny1 = m.ny + 1, nz1 = m.nz + 1;
   const int nn = (m.nx + 1) * ny1 * nz1;
-  double u[NC_COUNT];
+  if constexpr (KindTraits<KIND>::special) {
+    // the raw rows, as k_cell_rows forms them
+    double u[kMaxVc];
 #pragma unroll
-  for (int q = 0; q < NCMP; ++q) {
-    const double *f = F + ((long long)sl * NCMP + q) * nn;
-    double v[8];
+    for (int q = 0; q < NCMP; ++q) {
+      const double *f = F + ((long long)sl * NCMP + q) * nn;
+      double v[8];
 #pragma unroll
-    for (int c = 0; c < 8; ++c)
-      v[c] = f[((i + ((c >> 2) & 1)) * ny1 + (j + ((c >> 1) & 1))) * nz1 + (k + (c & 1))];
-    u[q + OFF] = combine8(q + OFF, v);
-  }
-  if (KIND == KIND_MAGNETIC) {
-    double raw[10];
-    raw_from_comps(KIND, u, mf, raw);
-#pragma unroll
-    for (int r = 0; r < 3; ++r) rows[((long long)sl * NS + r) * ld + cell] = (OutT)raw[r];
+      for (int c = 0; c < 8; ++c)
+        v[c] = f[((i + ((c >> 2) & 1)) * ny1 + (j + ((c >> 1) & 1))) * nz1 + (k + (c & 1))];
+      u[q] = combine8(KindTraits<KIND>::comp(q), v);
+    }
+    store_cell_rows<KIND, OutT>(u, mf, m.ngrid(), cell, rows + (long long)sl * NS * ld, ld);
   } else {
+    double u[NC_COUNT];
 #pragma unroll
-    for (int q = 0; q < NCMP; ++q) rows[((long long)sl * NS + q) * ld + cell] = (OutT)u[q + OFF];
+    for (int q = 0; q < NCMP; ++q) {
+      const double *f = F + ((long long)sl * NCMP + q) * nn;
+      double v[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        v[c] = f[((i + ((c >> 2) & 1)) * ny1 + (j + ((c >> 1) & 1))) * nz1 + (k + (c & 1))];
+      u[q + OFF] = combine8(q + OFF, v);
+    }
+    if (KIND == KIND_MAGNETIC) {
+      double raw[10];
+      raw_from_comps(KIND, u, mf, raw);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) rows[((long long)sl * NS + r) * ld + cell] = (OutT)raw[r];
+    } else {
+#pragma unroll
+      for (int q = 0; q < NCMP; ++q) rows[((long long)sl * NS + q) * ld + cell] = (OutT)u[q + OFF];
+    }
   }
 }
 
@@ -651,7 +668,7 @@ inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
   J3G_DISPATCH4(kind, CALL,                                                            \
                 case KIND_MAG_GRADIENT: { constexpr int K = KIND_MAG_GRADIENT; CALL; } break; \
                 case KIND_MAGNETIZATION: { constexpr int K = KIND_MAGNETIZATION; CALL; } break;)
-// the kinds with a node-component layout (stored sensitivity, node reduce)
+// the kinds with a node-component layout (node reduce)
 #define J3G_DISPATCH_ORDINARY(kind, CALL) J3G_DISPATCH4(kind, CALL, )
 
 cudaError_t launch_rho_tilde(const MeshView &m, const double *rho, double *rho_t,
@@ -764,7 +781,7 @@ cudaError_t launch_sens_rows(int kind, bool node_exact, const MeshView &m, const
 }
 
 int stored_rows_per_station(int kind) {
-  return kind_special(kind) ? 0 : kind == KIND_MAGNETIC ? 3 : kind_ncomp(kind);
+  return stored_rows(kind);
 }
 
 cudaError_t launch_stored_rows(int kind, const MeshView &m, const StationView &s, int s0, int ns,
@@ -773,10 +790,10 @@ cudaError_t launch_stored_rows(int kind, const MeshView &m, const StationView &s
   dim3 g1(cdiv(m.nnodes(), kThreads), ns);
   dim3 g2(cdiv(m.ngrid(), kThreads), ns);
   if (rows64) {
-    J3G_DISPATCH_ORDINARY(kind, (k_node_eval<K><<<g1, kThreads, 0, st>>>(m, s, s0, F),
+    J3G_DISPATCH(kind, (k_node_eval<K><<<g1, kThreads, 0, st>>>(m, s, s0, F),
                         k_cell_stored<K, double><<<g2, kThreads, 0, st>>>(m, F, mf, rows64, ld)));
   } else {
-    J3G_DISPATCH_ORDINARY(kind, (k_node_eval<K><<<g1, kThreads, 0, st>>>(m, s, s0, F),
+    J3G_DISPATCH(kind, (k_node_eval<K><<<g1, kThreads, 0, st>>>(m, s, s0, F),
                         k_cell_stored<K, float><<<g2, kThreads, 0, st>>>(m, F, mf, rows32, ld)));
   }
   return cudaGetLastError();

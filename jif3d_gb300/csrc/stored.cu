@@ -509,7 +509,7 @@ k_stored_assemble(int transform, double tbx, double tby, double tbz, int nmeas,
                   double *__restrict__ raw_out, double *__restrict__ data, long long ld_data) {
   constexpr int kind = KIND;
   constexpr int raw = kind_raw(kind);
-  constexpr int ns = kind == KIND_MAGNETIC ? 3 : kind_ncomp(kind);
+  constexpr int ns = stored_rows(kind);
   __shared__ double in_rec[kAsm * ns], out_rec[kAsm * raw];
   const int s0 = blockIdx.x * kAsm, n = blockIdx.y;
   const int count = min(kAsm, nmeas - s0), t = threadIdx.x, s = s0 + t;
@@ -518,9 +518,9 @@ k_stored_assemble(int transform, double tbx, double tby, double tbz, int nmeas,
   double r[10];
   if (t < count) {
     const double *sm = in_rec + t * ns;
-    if (kind == KIND_MAGNETIC) {
+    if constexpr (stored_is_raw(kind)) {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) r[c] = sm[c];
+      for (int c = 0; c < raw; ++c) r[c] = sm[c];
     } else {
       double u[NC_COUNT];
 #pragma unroll
@@ -566,7 +566,7 @@ k_stored_weights(int transform, double tbx, double tby, double tbz, int nmeas,
                  double *__restrict__ w_st, long long ld_w) {
   constexpr int kind = KIND;
   constexpr int raw = kind_raw(kind);
-  constexpr int ns = kind == KIND_MAGNETIC ? 3 : kind_ncomp(kind);
+  constexpr int ns = stored_rows(kind);
   __shared__ double raw_rec[kAsm * raw], st_rec[kAsm * ns];
   const int s0 = blockIdx.x * kAsm, n = blockIdx.y;
   const int count = min(kAsm, nmeas - s0), t = threadIdx.x, s = s0 + t;
@@ -594,9 +594,9 @@ k_stored_weights(int transform, double tbx, double tby, double tbz, int nmeas,
     }
 #pragma unroll
     for (int c = 0; c < raw; ++c) raw_rec[t * raw + c] = w[c];
-    if (kind == KIND_MAGNETIC) {
+    if constexpr (stored_is_raw(kind)) {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) st_rec[t * ns + c] = w[c];
+      for (int c = 0; c < raw; ++c) st_rec[t * ns + c] = w[c];
     } else {
       double u[NC_COUNT];
       comps_from_raw_weights(kind, w, mf, u);
@@ -748,6 +748,8 @@ cudaError_t launch_stored_assemble(int kind, int transform, double tbx, double t
     case KIND_TENSOR: J3G_ASSEMBLE(KIND_TENSOR); break;
     case KIND_MAGNETIC: J3G_ASSEMBLE(KIND_MAGNETIC); break;
     case KIND_JOINT: J3G_ASSEMBLE(KIND_JOINT); break;
+    case KIND_MAG_GRADIENT: J3G_ASSEMBLE(KIND_MAG_GRADIENT); break;
+    case KIND_MAGNETIZATION: J3G_ASSEMBLE(KIND_MAGNETIZATION); break;
     default: return cudaErrorInvalidValue;
   }
 #undef J3G_ASSEMBLE
@@ -768,6 +770,8 @@ cudaError_t launch_stored_weights(int kind, int transform, double tbx, double tb
     case KIND_TENSOR: J3G_WEIGHTS(KIND_TENSOR); break;
     case KIND_MAGNETIC: J3G_WEIGHTS(KIND_MAGNETIC); break;
     case KIND_JOINT: J3G_WEIGHTS(KIND_JOINT); break;
+    case KIND_MAG_GRADIENT: J3G_WEIGHTS(KIND_MAG_GRADIENT); break;
+    case KIND_MAGNETIZATION: J3G_WEIGHTS(KIND_MAGNETIZATION); break;
     default: return cudaErrorInvalidValue;
   }
 #undef J3G_WEIGHTS

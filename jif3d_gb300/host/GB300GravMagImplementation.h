@@ -148,6 +148,46 @@ class GB300GravMagImplementation : public ThreeDGravMagImplementation<DataType> 
     return ToRvec(grad);
   }
 
+  // -- Device-resident sensitivities (GB300DeviceSensitivityCalculator) ----
+  // Loads the model's geometry and the stations (nothing is sent when they
+  // are unchanged; any change drops the stored J) and tells whether J is
+  // held in HBM in `storage` (J3G_STORE_FP32 / J3G_STORE_F16X2) for them.
+  bool HasStoredSensitivity(const ModelType &Model, const DataType &Data, int storage) {
+    Upload(ctx_, Model, Data, Data.GetMeasPosX().size(), 0);
+    CheckTransform();
+    int have = 0;
+    Check(ctx_, j3g_sensitivity_info(ctx_, &have, nullptr, nullptr, nullptr),
+          "j3g_sensitivity_info");
+    return have == storage;
+  }
+  // Builds J for the geometry last loaded by HasStoredSensitivity.
+  void BuildStoredSensitivity(int storage) {
+    Check(ctx_, j3g_build_sensitivity(ctx_, storage), "j3g_build_sensitivity");
+  }
+  // nmodels models [nmodels][nparm] -> data [nmodels][nmeas * data per
+  // station] with the stored J (the geometry of the last
+  // HasStoredSensitivity call).
+  std::vector<double> StoredForward(const std::vector<double> &models, int nmodels) {
+    int nmeas = 0, dpm = 0;
+    Check(ctx_, j3g_get_sizes(ctx_, nullptr, nullptr, &nmeas, nullptr, &dpm), "j3g_get_sizes");
+    std::vector<double> data((size_t)nmodels * nmeas * dpm);
+    Check(ctx_, j3g_batched_forward(ctx_, nmodels, models.data(), data.data()),
+          "j3g_batched_forward");
+    return data;
+  }
+  // Gradients [nmodels][nparm] of the misfits [nmodels][nmeas * data per
+  // station] at the models, with the stored J.
+  std::vector<double> StoredLQDerivative(const std::vector<double> &models,
+                                         const std::vector<double> &misfits, int nmodels) {
+    long long nparm = 0;
+    Check(ctx_, j3g_get_sizes(ctx_, nullptr, &nparm, nullptr, nullptr, nullptr), "j3g_get_sizes");
+    std::vector<double> grads((size_t)nmodels * nparm);
+    Check(ctx_, j3g_batched_lqderivative(ctx_, nmodels, models.data(), misfits.data(),
+                                         grads.data()),
+          "j3g_batched_lqderivative");
+    return grads;
+  }
+
  private:
   // Per-station parts of the base class's station loop, through a context
   // holding the one station: the gridded response and rows (columns of the

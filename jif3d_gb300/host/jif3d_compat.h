@@ -232,6 +232,11 @@ class ThreeDGravMagCalculator {
   virtual void HandleSensitivities(const size_t measindex) = 0;
 
  protected:
+  // the cell values match the cell sizes (ThreeDGravMagCalculator.h:122-145)
+  void CheckModelConsistency(const ModelType &Model) {
+    if (Model.GetData().size() != Model.NCells())
+      throw FatalException("Model values do not match the cell sizes");
+  }
   rmat CurrentSensitivities;
   std::shared_ptr<VectorTransform> Transform;
   std::shared_ptr<ThreeDGravMagImplementation<DataType>> Imp;

@@ -15,12 +15,19 @@
 //   minmem (MinMem calculator), full (FullSensitivity calculator), rows
 //   (its sensitivity matrix, row-major), grad (LQDerivative), loop (the base
 //   class's per-station loop, no transform only), and "exception ok" when a
-//   wrong misfit size raised FatalException.
+//   wrong misfit size raised FatalException.  Then the device-resident
+//   calculator (GB300DeviceSensitivityCalculator, fp16 hi / lo storage):
+//   devfirst (first call, FP64), devcached (second call, stored J), devgrad,
+//   devbatch / devbatchgrad (rows k = 0, 1, 2: the model times 1 + 0.1 k and
+//   the misfit times k + 1), devmoved (station 0 moved by +1 m in x: a new
+//   geometry, FP64 again) and "devexception ok" for a misfit row count that
+//   does not match the models.
 #define JIF3D_GB300_STANDALONE
 #include <cstdio>
 #include <fstream>
 #include <memory>
 
+#include "GB300DeviceSensitivityCalculator.h"
 #include "GB300GravMagImplementation.h"
 
 using namespace jif3D;
@@ -59,6 +66,13 @@ Problem read_problem(const char *path) {
   p.misfit = read_vec(in, n);
   if (!in) throw FatalException("cannot read the problem file");
   return p;
+}
+
+rvec flatten(const rmat &m) {
+  rvec v(m.size1() * m.size2());
+  for (size_t r = 0; r < m.size1(); ++r)
+    for (size_t c = 0; c < m.size2(); ++c) v(r * m.size2() + c) = m(r, c);
+  return v;
 }
 
 void put(std::FILE *f, const char *name, const rvec &v) {
@@ -134,6 +148,29 @@ void run(const Problem &p, std::shared_ptr<GB300GravMagImplementation<DataType>>
     minmem.LQDerivative(model, data, rvec(mis.size() + 1));
   } catch (const FatalException &) {
     std::fprintf(out, "exception ok\n");
+  }
+
+  GB300DeviceSensitivityCalculator<DataType> dev(imp, J3G_STORE_F16X2);
+  if (auto t = transform_of(p.transform)) dev.SetDataTransform(t);
+  put(out, "devfirst", dev.Calculate(model, data));
+  put(out, "devcached", dev.Calculate(model, data));
+  put(out, "devgrad", dev.LQDerivative(model, data, mis));
+  const rvec params = model.GetModelParameters();
+  rmat P(3, params.size()), M(3, mis.size());
+  for (size_t k = 0; k < 3; ++k) {
+    for (size_t c = 0; c < params.size(); ++c) P(k, c) = params(c) * (1.0 + 0.1 * k);
+    for (size_t c = 0; c < mis.size(); ++c) M(k, c) = mis(c) * (k + 1.0);
+  }
+  put(out, "devbatch", flatten(dev.CalculateBatch(model, data, P)));
+  put(out, "devbatchgrad", flatten(dev.LQDerivativeBatch(model, data, P, M)));
+  DataType moved;
+  for (size_t i = 0; i + 2 < p.st.size(); i += 3)
+    moved.AddMeasurementPoint(p.st[i] + (i == 0 ? 1.0 : 0.0), p.st[i + 1], p.st[i + 2]);
+  put(out, "devmoved", dev.Calculate(model, moved));
+  try {
+    dev.LQDerivativeBatch(model, data, P, rmat(2, mis.size()));
+  } catch (const FatalException &) {
+    std::fprintf(out, "devexception ok\n");
   }
 }
 

@@ -3,7 +3,11 @@ driven through jif3D-style calculators by tests/cpp/host_adapter_check.cpp:
 MinMem and FullSensitivity calculators, LQDerivative, the base class's
 per-station loop over CalcGridded / CalcBackground, and the FatalException on
 a bad misfit size -- compared with the oracle at the FP64 tolerance (relative
-norm error <= 1e-10)."""
+norm error <= 1e-10) -- and the device-resident calculator
+(jif3d_gb300/host/GB300DeviceSensitivityCalculator.h): its FP64 first call,
+stored-J calls and batches at the mixed-path tolerance (1e-6), and a moved
+station that must not hit the cache."""
+import dataclasses
 import os
 import subprocess
 
@@ -16,7 +20,7 @@ from jif3d_gb300 import build as B, workloads as W
 pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-TOL = 1e-10
+TOL, TOL_MIXED = 1e-10, 1e-6
 
 
 @pytest.fixture(scope="module")
@@ -48,8 +52,8 @@ def read_output(path):
     with open(path) as f:
         for line in f:
             parts = line.split()
-            if parts[:2] == ["exception", "ok"]:
-                out["exception"] = True
+            if parts[1:2] == ["ok"]:
+                out[parts[0]] = True
                 continue
             out[parts[0]] = np.array([float(v) for v in parts[2:]])
             assert out[parts[0]].size == int(parts[1])
@@ -83,3 +87,17 @@ def test_cpp_implementation(oracle_lib, exe, tmp_path, kind, transform):
     if transform == W.T_NONE:  # the per-station loop (stand-in base class, no transform)
         assert relerr(o["loop"], dref) <= TOL
         assert relerr(o["looprows"], Jref.ravel()) <= TOL
+    # the device-resident calculator: FP64 first call, then the stored J
+    assert relerr(o["devfirst"], dref) <= TOL
+    assert relerr(o["devcached"], dref) <= TOL_MIXED
+    assert relerr(o["devgrad"], gref) <= TOL_MIXED
+    batch, bgrad = o["devbatch"].reshape(3, -1), o["devbatchgrad"].reshape(3, -1)
+    for k in range(3):
+        mk = s.model * (1.0 + 0.1 * k)
+        assert relerr(batch[k], oracle_forward(oracle_lib, s, mk)) <= TOL_MIXED
+        assert relerr(bgrad[k], oracle_lqderivative(oracle_lib, s, misfit * (k + 1.0), mk)) \
+            <= TOL_MIXED
+    moved = dataclasses.replace(s, stations=s.stations.copy())
+    moved.stations[0, 0] += 1.0
+    assert relerr(o["devmoved"], oracle_forward(oracle_lib, moved)) <= TOL
+    assert o.get("devexception")

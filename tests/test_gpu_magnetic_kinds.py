@@ -5,7 +5,9 @@ Tolerance (FP64 path): relative norm error <= 1e-10 per output group, as for
 the other kinds.  Both kinds run through the node-term kernels (virtual
 components: the gradient evaluates every node at the station and 1 m below
 it; magnetisation accumulates U_kj against three model blocks) and through
-the eight-corner path when the mesh corners are not running sums.
+the eight-corner path when the mesh corners are not running sums.  Their
+device-resident sensitivity (batched stored products) is checked at the
+mixed-path tolerance, 1e-6.
 """
 import numpy as np
 import pytest
@@ -82,11 +84,37 @@ def test_corner_path(ctx, oracle_lib, kind):
     assert relerr(c.lqderivative(s.model, misfit), p.lqderivative(s.model, misfit)) <= TOL
 
 
-def test_unsupported_combinations(ctx):
-    s = survey(W.MAGNETIZATION, seed=360)
+STORED_CASES = [(W.MAG_GRADIENT, W.T_NONE), (W.MAGNETIZATION, W.T_NONE),
+                (W.MAGNETIZATION, W.T_TOTAL_FIELD), (W.MAGNETIZATION, W.T_TFA)]
+
+
+@pytest.mark.parametrize("storage", [capi.STORE_FP32, capi.STORE_F16X2])
+@pytest.mark.parametrize("kind,transform", STORED_CASES)
+def test_stored_sensitivity(ctx, oracle_lib, kind, transform, storage):
+    """Device-resident J of both kinds (raw rows: 1 per station for the
+    gradient, 3 over the three magnetisation blocks): batched products
+    against the oracle at the mixed-path tolerance, 1e-6."""
+    s = survey(kind, seed=380 + 10 * kind + transform, transform=transform, nx=9, ny=8, nz=6,
+               nmeas=13)
     c = setup(ctx, s)
-    with pytest.raises(capi.J3GError):  # no device-resident sensitivity for these kinds
-        c.build_sensitivity(capi.STORE_FP32)
+    c.build_sensitivity(storage)
+    info = c.sensitivity_info()
+    assert info["storage"] == storage
+    assert info["cols"] == (3 if kind == W.MAGNETIZATION else 1) * s.ngrid
+    rng = np.random.default_rng(kind + transform)
+    models = s.model[None, :] * (1 + 0.2 * rng.normal(size=(4, s.nparm)))
+    d = c.batched_forward(models)
+    mis = rng.normal(size=d.shape)
+    g = c.batched_lqderivative(models, mis)
+    for i in range(models.shape[0]):
+        assert relerr(d[i], oracle_forward(oracle_lib, s, models[i])) <= 1e-6
+        gref = oracle_lqderivative(oracle_lib, s, mis[i], models[i])
+        assert relerr(g[i], gref) <= 1e-6
+        if kind == W.MAG_GRADIENT:
+            assert np.all(g[i, s.ngrid:] == 0.0)  # background parameters: no response
+
+
+def test_unsupported_combinations(ctx):
     g = survey(W.MAG_GRADIENT, seed=361)
     c = setup(ctx, g)
     with pytest.raises(capi.J3GError):  # the gradient has no total-field transform
