@@ -183,6 +183,45 @@ def timed_steps(step, nsteps, stream, flush):
     return times
 
 
+def host_link(h_in, h_out, stream):
+    """Host link speed from page-locked buffers (best of 5): the input
+    buffer copied in, the output buffer copied out, and both at once on two
+    streams (GB/s of all bytes moved)."""
+    import torch
+    d_in = torch.empty_like(h_in, device="cuda")
+    d_out = torch.empty_like(h_out, device="cuda")
+    s2 = torch.cuda.Stream()
+    nb_in, nb_out = h_in.numel() * 8, h_out.numel() * 8
+
+    def best(fn, nbytes):
+        t = []
+        for _ in range(5):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            t.append(time.perf_counter() - t0)
+        return nbytes / min(t) / 1e9
+
+    def h2d():
+        with torch.cuda.stream(stream):
+            d_in.copy_(h_in, non_blocking=True)
+
+    def d2h():
+        with torch.cuda.stream(s2):
+            h_out.copy_(d_out, non_blocking=True)
+
+    def both():
+        h2d()
+        d2h()
+    r = {"h2d_gbs": best(h2d, nb_in), "d2h_gbs": best(d2h, nb_out),
+         "both_gbs": best(both, nb_in + nb_out),
+         "how": "torch copies of the pinned step buffers (models in, gradients out), "
+                "alone and on two streams at once; best of 5"}
+    del d_in, d_out
+    return r
+
+
 def measure_refinement(s, nmod, steps, stream, flush, local, peaks):
     """ProjectValues and CombineGradient of the batch between the inversion
     grid of the workload (coarse) and a forward grid refined 2 x 2 x 2; each
@@ -402,23 +441,26 @@ def run_batched(args, rank, world, local):
                                      out=st["grads"].numpy())
 
     def e2e_pipelined(nsteps):
-        """Step i queues the forward of step i + 1, waits for its own data,
-        forms the misfit and queues its derivative; the gradient of step i - 1
-        is taken (waited for) after that, as an optimiser would use it."""
+        """Step i waits for its own data, forms the misfit, queues its
+        derivative and then the forward of step i + 2 (the batches' models are
+        known ahead, as for independent batches); the gradient of step i - 1
+        is taken (waited for) last.  The forward's 268 MB model copy so gets
+        two products of lead time, and at most four calls are in flight."""
         fwd, adj = {}, {}
 
         def queue_fwd(i):
             st = sets[i % 2]
             fwd[i] = ctx.batched_forward_async(st["models"].numpy(), out=st["data"].numpy())
-        queue_fwd(0)
+        for i in range(min(2, nsteps)):
+            queue_fwd(i)
         for i in range(nsteps):
             st = sets[i % 2]
-            if i + 1 < nsteps:
-                queue_fwd(i + 1)
             ctx.batched_wait(fwd[i])
             misfit(st)
             adj[i] = ctx.batched_lqderivative_async(st["models"].numpy(), st["mis"].numpy(),
                                                     out=st["grads"].numpy())
+            if i + 2 < nsteps:
+                queue_fwd(i + 2)
             if i >= 1:
                 ctx.batched_wait(adj[i - 1])
         ctx.batched_wait(adj[nsteps - 1])
@@ -435,11 +477,14 @@ def run_batched(args, rank, world, local):
     e2e_s = max_over_ranks(t2 - t1, world)
     nbytes_in = 8 * (s.models.size + data.numel())
     nbytes_out = 8 * (data.numel() + s.models.size)
+    link = host_link(sets[0]["models"], sets[1]["grads"], stream)
+    link["bound_ms_per_step"] = (nbytes_in + nbytes_out) / (link["both_gbs"] * 1e6)
     e2e = {"value": units * world * args.steps / e2e_s / 1e6, "unit": UNIT,
            "h2d_bytes_per_step": nbytes_in, "host_buffers": "pinned",
-           "d2h_bytes_per_step": nbytes_out,
-           "how": "pipelined calls (j3g_batched_*_async): the next step's forward is queued "
-                  "before this step's misfit; copies on their own streams overlap the products",
+           "d2h_bytes_per_step": nbytes_out, "ms_per_step": e2e_s * 1e3 / args.steps,
+           "link": link,
+           "how": "pipelined calls (j3g_batched_*_async): each step's forward is queued two "
+                  "steps ahead; copies on their own streams overlap the products",
            "blocking": {"value": units * world * args.steps / sync_s / 1e6,
                         "how": "j3g_batched_forward / j3g_batched_lqderivative, one at a time"}}
 

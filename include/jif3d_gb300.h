@@ -250,8 +250,9 @@ int j3g_batched_lqderivative(j3g_context *ctx, int nmodels, const double *h_mode
  * the product and the copy of its output back, and returns a ticket; the
  * copies run on two streams of the context's own (in, out), so they overlap
  * the products of the calls before and after.  j3g_batched_wait(ticket)
- * blocks until that call's output is in host memory.  Up to three calls are
- * in flight (a fourth waits for the first); the host buffers must stay
+ * blocks until that call's output is in host memory.  Up to four calls are
+ * in flight (a fifth waits for the first: enough to queue a forward two
+ * steps ahead of the misfit it feeds); the host buffers must stay
  * valid and unchanged until the call is waited for, and page-locked host
  * buffers are needed for the copies to overlap. */
 int j3g_batched_forward_async(j3g_context *ctx, int nmodels, const double *h_models,

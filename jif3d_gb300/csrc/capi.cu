@@ -111,7 +111,7 @@ struct j3g_context {
     int *flag = nullptr;    // page-locked copy of the tensor-core error flag
     long long ticket = -1;  // call in flight in this slot, -1 if free
   };
-  static constexpr int kSlots = 3;
+  static constexpr int kSlots = 4;
   Slot slots[kSlots];
   cudaStream_t h2d_stream = nullptr, d2h_stream = nullptr;
   long long next_ticket = 0;

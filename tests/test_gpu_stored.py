@@ -134,7 +134,7 @@ def test_batched_host_pinned_outputs(ctx):
 @pytest.mark.parametrize("kind,transform", [(W.JOINT, W.T_NONE), (W.TENSOR, W.T_FTG_INVARIANT)])
 def test_pipelined_batched_calls(ctx, kind, transform):
     """The pipelined host-buffer calls give, bit for bit, what the blocking
-    calls give: four forwards in flight (the ring holds three), waits out of
+    calls give: five forwards in flight (the ring holds four), waits out of
     order, derivatives with and without the models (the FTG invariant needs
     them), page-locked and pageable buffers."""
     import torch
@@ -148,7 +148,7 @@ def test_pipelined_batched_calls(ctx, kind, transform):
 
     def pinned(shape):
         return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
-    batches = [s.model[None, :] * rng.uniform(0.5, 1.5, (3, s.nparm)) for _ in range(4)]
+    batches = [s.model[None, :] * rng.uniform(0.5, 1.5, (3, s.nparm)) for _ in range(5)]
     outs = [pinned((3, nd)) for _ in batches]
     tickets = [ctx.batched_forward_async(b, out=o) for b, o in zip(batches, outs)]
     for t in reversed(tickets):
@@ -164,6 +164,7 @@ def test_pipelined_batched_calls(ctx, kind, transform):
     ctx.batched_wait(tickets[1])
     ctx.batched_wait(t_fwd)
     ctx.batched_wait(tickets[3])
+    ctx.batched_wait(tickets[4])
     ctx.batched_wait(tickets[0])  # its slot was reused: already complete
     for b, r, g in zip(batches, mis, grads):
         assert np.array_equal(g, ctx.batched_lqderivative(b, r))
