@@ -264,6 +264,61 @@ def measure_refinement(s, nmod, steps, stream, flush, local, peaks):
     return out
 
 
+def measure_stream(steps, stream, flush, local, peaks):
+    """The FTG survey on the 64 x 64 x 32 mesh with 40 x 40 stations: the
+    forward and adjoint of one model through the FP32 device-resident J (six
+    stored rows per station: 9600 x 131072, 5.03 GB), each streaming J once
+    (k_gemv_f32 / k_gemv_t_f32), timed alone with CUDA events, L2 flushed in
+    between; next to the FP64 matrix-free path on the same survey, and the
+    FP32 products' errors against it."""
+    import torch
+    from jif3d_gb300 import capi, workloads as W
+    s = W.config2()
+    ctx = capi.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    W.setup_context(ctx, s)
+    dev = f"cuda:{local}"
+    n = s.stations.shape[0]
+    nd = n * s.dpm
+    m = torch.tensor(s.model, dtype=torch.float64, device=dev)
+    r = torch.tensor(np.random.default_rng(12).normal(size=nd), dtype=torch.float64, device=dev)
+    d64, d32 = (torch.zeros(nd, dtype=torch.float64, device=dev) for _ in range(2))
+    g64, g32 = (torch.zeros(s.nparm, dtype=torch.float64, device=dev) for _ in range(2))
+
+    def plain():
+        ctx.forward_device(m.data_ptr(), d64.data_ptr())
+        ctx.lqderivative_device(m.data_ptr(), r.data_ptr(), g64.data_ptr())
+    plain()
+    t_plain = statistics.median(timed_steps(plain, 2, stream, flush))
+    ctx.build_sensitivity(capi.STORE_FP32)
+    info = ctx.sensitivity_info()
+    fwd = lambda: ctx.stored_forward_device(m.data_ptr(), d32.data_ptr())
+    adj = lambda: ctx.stored_lqderivative_device(m.data_ptr(), r.data_ptr(), g32.data_ptr())
+    for _ in range(3):
+        fwd()
+        adj()
+    torch.cuda.synchronize()
+    t_f = statistics.median(timed_steps(fwd, steps, stream, flush))
+    t_a = statistics.median(timed_steps(adj, steps, stream, flush))
+    jb = info["bytes"]
+    relerr = lambda x, y: float(torch.linalg.norm(x - y) / torch.linalg.norm(y))
+    out = {"workload": s.name + "_fp32_stored", "cells": s.ngrid, "stations": n,
+           "stored_rows": info["rows"], "j_bytes": jb,
+           "value": s.ngrid * n / ((t_f + t_a) * 1e-3) / 1e6, "unit": UNIT,
+           "forward_ms": t_f, "adjoint_ms": t_a,
+           "forward_gbs": jb / (t_f * 1e-3) / 1e9, "adjoint_gbs": jb / (t_a * 1e-3) / 1e9,
+           "hbm_peak_gbs": peaks["hbm_gbs"],
+           "plain_fp64": {"value": s.ngrid * n / (t_plain * 1e-3) / 1e6, "ms_per_step": t_plain},
+           "err_vs_fp64": {"data": relerr(d32, d64), "grad": relerr(g32, g64)},
+           "how": "J streamed once per direction (algorithmic bytes = J bytes); times include "
+                  "the model conversion, the chunk sums and the assembly / weights kernels"}
+    out["forward_frac"] = out["forward_gbs"] / peaks["hbm_gbs"]
+    out["adjoint_frac"] = out["adjoint_gbs"] / peaks["hbm_gbs"]
+    out["speedup_vs_plain_fp64"] = out["value"] / out["plain_fp64"]["value"]
+    ctx.close()
+    return out
+
+
 def measure_netcdf(s, data):
     """Host throughput of the library's NetCDF writer and reader on the
     workload's files: the density model (131,072 cells) and the FTG data of
@@ -512,6 +567,7 @@ def run_batched(args, rank, world, local):
             "hbm_peak_gbs": peaks["hbm_gbs"]}
     ctx.close()
     refinement = measure_refinement(s, nmod, args.steps, stream, flush, local, peaks)
+    stream_fp32 = measure_stream(args.steps, stream, flush, local, peaks)
     ftg = data[0].view(n, 10)[:, 1:].reshape(-1).cpu().numpy()
     netcdf_io = measure_netcdf(s, ftg) if rank == 0 else None
     return {
@@ -534,7 +590,7 @@ def run_batched(args, rank, world, local):
         "step": "one CUDA graph per step (batched forward, weighted misfit, batched "
                 "adjoint: %d library kernels + 2 torch kernels), replayed" % launches_per_step,
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "clocks": clk,
-        "refinement": refinement, "netcdf": netcdf_io,
+        "refinement": refinement, "stream_fp32": stream_fp32, "netcdf": netcdf_io,
     }
 
 

@@ -292,11 +292,17 @@ __global__ void __launch_bounds__(kT) k_gemv_f32(const float *__restrict__ J, lo
 }
 
 // part[chunk][c] = sum_{r in chunk} J[r][c] w[r]; block = 1024 columns x RC rows.
+// Rows go in groups of 16: the group's 16 float4 loads are issued together
+// (a thread keeps 256 bytes in flight), then summed in row order in an FP32
+// chain that is added into the FP64 column sums once per group.
 constexpr int kRC = 128;
+constexpr int kRG = 16;  // rows per FP32 chain and per load batch
+static_assert(kRC % kRG == 0, "chunks are whole row groups");
 __global__ void __launch_bounds__(kT) k_gemv_t_f32(const float *__restrict__ J, long long ld,
                                                    int nrows, const double *__restrict__ w,
                                                    double *__restrict__ part) {
   const long long c4 = (long long)blockIdx.x * kT + threadIdx.x;  // float4 column index
+  const bool active = c4 * 4 < ld;
   const int nchunk = (nrows + kRC - 1) / kRC;
   __shared__ float ws[kRC];
   // row chunks loop over grid y (at most 65535 blocks)
@@ -305,24 +311,29 @@ __global__ void __launch_bounds__(kT) k_gemv_t_f32(const float *__restrict__ J, 
     __syncthreads();  // the previous chunk's weights are no longer read
     for (int t = threadIdx.x; t < kRC; t += kT) ws[t] = (r0 + t < r1) ? (float)w[r0 + t] : 0.0f;
     __syncthreads();
-    if (c4 * 4 >= ld) continue;
+    if (!active) continue;
     double d0 = 0, d1 = 0, d2 = 0, d3 = 0;
-    float f0 = 0, f1 = 0, f2 = 0, f3 = 0;
-    int cnt = 0;
-    for (int r = r0; r < r1; ++r) {
-      const float4 a = __ldcs(reinterpret_cast<const float4 *>(J + (long long)r * ld) + c4);
-      const float wr = ws[r - r0];
-      f0 = fmaf(a.x, wr, f0);
-      f1 = fmaf(a.y, wr, f1);
-      f2 = fmaf(a.z, wr, f2);
-      f3 = fmaf(a.w, wr, f3);
-      if (++cnt == 16) {
-        d0 += f0; d1 += f1; d2 += f2; d3 += f3;
-        f0 = f1 = f2 = f3 = 0.0f;
-        cnt = 0;
+    const float4 *col = reinterpret_cast<const float4 *>(J) + c4;
+    const long long ld4 = ld / 4;
+    for (int g = r0; g < r1; g += kRG) {
+      const int ng = min(kRG, r1 - g);
+      float4 a[kRG];
+#pragma unroll
+      for (int u = 0; u < kRG; ++u)
+        a[u] = u < ng ? __ldcs(col + (long long)(g + u) * ld4) : make_float4(0.f, 0.f, 0.f, 0.f);
+      float f0 = 0, f1 = 0, f2 = 0, f3 = 0;
+#pragma unroll
+      for (int u = 0; u < kRG; ++u) {
+        if (u < ng) {
+          const float wr = ws[g - r0 + u];
+          f0 = fmaf(a[u].x, wr, f0);
+          f1 = fmaf(a[u].y, wr, f1);
+          f2 = fmaf(a[u].z, wr, f2);
+          f3 = fmaf(a[u].w, wr, f3);
+        }
       }
+      d0 += f0; d1 += f1; d2 += f2; d3 += f3;
     }
-    d0 += f0; d1 += f1; d2 += f2; d3 += f3;
     double *o = part + (long long)chunk * ld + c4 * 4;
     o[0] = d0; o[1] = d1; o[2] = d2; o[3] = d3;
   }
