@@ -292,13 +292,14 @@ __global__ void __launch_bounds__(kT) k_gemv_f32(const float *__restrict__ J, lo
 }
 
 // part[chunk][c] = sum_{r in chunk} J[r][c] w[r]; block = 1024 columns x RC rows.
-// Rows go in groups of 16: the group's 16 float4 loads are issued together
-// (a thread keeps 256 bytes in flight), then summed in row order in an FP32
-// chain that is added into the FP64 column sums once per group.
+// Rows go in groups of 16, summed in row order in an FP32 chain that is added
+// into the FP64 column sums once per group; a group's loads are issued in
+// batches of 8 float4 (128 bytes in flight per thread, four blocks per SM).
 constexpr int kRC = 128;
-constexpr int kRG = 16;  // rows per FP32 chain and per load batch
-static_assert(kRC % kRG == 0, "chunks are whole row groups");
-__global__ void __launch_bounds__(kT) k_gemv_t_f32(const float *__restrict__ J, long long ld,
+constexpr int kRG = 16;  // rows per FP32 chain
+constexpr int kRB = 8;   // rows per load batch
+static_assert(kRC % kRG == 0 && kRG % kRB == 0, "chunks are whole row groups and batches");
+__global__ void __launch_bounds__(kT, 4) k_gemv_t_f32(const float *__restrict__ J, long long ld,
                                                    int nrows, const double *__restrict__ w,
                                                    double *__restrict__ part) {
   const long long c4 = (long long)blockIdx.x * kT + threadIdx.x;  // float4 column index
@@ -316,20 +317,24 @@ __global__ void __launch_bounds__(kT) k_gemv_t_f32(const float *__restrict__ J, 
     const float4 *col = reinterpret_cast<const float4 *>(J) + c4;
     const long long ld4 = ld / 4;
     for (int g = r0; g < r1; g += kRG) {
-      const int ng = min(kRG, r1 - g);
-      float4 a[kRG];
-#pragma unroll
-      for (int u = 0; u < kRG; ++u)
-        a[u] = u < ng ? __ldcs(col + (long long)(g + u) * ld4) : make_float4(0.f, 0.f, 0.f, 0.f);
       float f0 = 0, f1 = 0, f2 = 0, f3 = 0;
 #pragma unroll
-      for (int u = 0; u < kRG; ++u) {
-        if (u < ng) {
-          const float wr = ws[g - r0 + u];
-          f0 = fmaf(a[u].x, wr, f0);
-          f1 = fmaf(a[u].y, wr, f1);
-          f2 = fmaf(a[u].z, wr, f2);
-          f3 = fmaf(a[u].w, wr, f3);
+      for (int h = 0; h < kRG; h += kRB) {
+        const int nb = min(kRB, r1 - g - h);  // rows of this batch (<= 0: none)
+        float4 a[kRB];
+#pragma unroll
+        for (int u = 0; u < kRB; ++u)
+          a[u] = u < nb ? __ldcs(col + (long long)(g + h + u) * ld4)
+                        : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < kRB; ++u) {
+          if (u < nb) {
+            const float wr = ws[g - r0 + h + u];
+            f0 = fmaf(a[u].x, wr, f0);
+            f1 = fmaf(a[u].y, wr, f1);
+            f2 = fmaf(a[u].z, wr, f2);
+            f3 = fmaf(a[u].w, wr, f3);
+          }
         }
       }
       d0 += f0; d1 += f1; d2 += f2; d3 += f3;
