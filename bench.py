@@ -44,6 +44,9 @@ SIGMA_GZ, SIGMA_U = 1e-8, 1e-9
 # measured by ncu on the probe kernels: sqrt 13, flog 21, fatan2 36, pair 42
 # (profiles/fp64_weights.md); the node kernels' own counters give 223 / 214.
 FP64_FLOP_PER_JOINT_NODE = 225.0
+# FP64 flops per node evaluation of the other kinds, counted by ncu
+# (DFMA = 2, DADD, DMUL) on the node kernels, mean of forward and adjoint
+FP64_FLOP_PER_NODE = {1: 110.0, 2: 210.0, 3: 208.0, 4: FP64_FLOP_PER_JOINT_NODE}
 
 
 def parse():
@@ -319,6 +322,67 @@ def measure_stream(steps, stream, flush, local, peaks):
     return out
 
 
+def measure_fp64_configs(stream, flush, local):
+    """The FP64 matrix-free forward + adjoint of one model on the other
+    workloads, timed with CUDA events (L2 flushed in between): g_z on the
+    30 x 30 x 15 mesh (400 stations, 3 background layers), joint g_z + FTG on
+    96 x 96 x 48 (2500 stations) and the total-field anomaly on 128 x 128 x 64
+    through the uneven station subsets (the first two of the 32; all 32
+    would take ~45 s).  FP64 roofline: node evaluations x FP64 flops per node
+    of the kind / time against the measured FP64 FMA rate."""
+    import torch
+    from jif3d_gb300 import capi, workloads as W
+    dev = f"cuda:{local}"
+    out = {}
+    peak = None
+    for cfg, nsub, nsteps in ((1, 0, 5), (3, 0, 2), (5, 2, 1)):
+        s = W.CONFIGS[cfg]()
+        ctx = capi.Context(local)
+        ctx.set_stream(stream.cuda_stream)
+        W.setup_context(ctx, s)
+        peak = peak or ctx.probe_fp64()
+        m = torch.tensor(s.model, dtype=torch.float64, device=dev)
+        rng = np.random.default_rng(cfg)
+        if nsub:
+            subs = s.subsets[:nsub]
+            nst = sum(len(x) for x in subs)
+            nd = nst * s.dpm
+            d = torch.zeros(nd, dtype=torch.float64, device=dev)
+            r = torch.tensor(rng.normal(size=nd), dtype=torch.float64, device=dev)
+            g = torch.zeros((nsub, s.nparm), dtype=torch.float64, device=dev)
+
+            def step():
+                ctx.subsets_forward_device(subs, m.data_ptr(), d.data_ptr())
+                ctx.subsets_lqderivative_device(subs, m.data_ptr(), r.data_ptr(), g.data_ptr())
+        else:
+            nst = s.stations.shape[0]
+            nd = nst * s.dpm
+            d = torch.zeros(nd, dtype=torch.float64, device=dev)
+            r = torch.tensor(rng.normal(size=nd), dtype=torch.float64, device=dev)
+            g = torch.zeros(s.nparm, dtype=torch.float64, device=dev)
+
+            def step():
+                ctx.forward_device(m.data_ptr(), d.data_ptr())
+                ctx.lqderivative_device(m.data_ptr(), r.data_ptr(), g.data_ptr())
+        step()
+        torch.cuda.synchronize()
+        t = statistics.median(timed_steps(step, nsteps, stream, flush))
+        nodes = (s.shape[0] + 1) * (s.shape[1] + 1) * (s.shape[2] + 1)
+        kind = s.kind  # scalar 1, tensor 2, magnetic 3, joint 4
+        gflops = 2 * nodes * nst * FP64_FLOP_PER_NODE[kind] / (t * 1e-3) / 1e9
+        out[s.name] = {"cells": s.ngrid, "stations": nst, "ms_per_step": t,
+                       "value": s.ngrid * nst / (t * 1e-3) / 1e6, "unit": UNIT,
+                       "fp64_gflops": gflops, "fp64_frac": gflops / peak,
+                       "flop_per_node": FP64_FLOP_PER_NODE[kind]}
+        if nsub:
+            out[s.name]["subsets"] = [len(x) for x in subs]
+        ctx.close()
+    out["fp64_peak_gflops"] = peak
+    out["how"] = ("forward + adjoint of one model per step; fp64_frac counts node evaluations "
+                  "only (the background, reductions and assembly are in the time)")
+    return out
+
+
 def measure_netcdf(s, data):
     """Host throughput of the library's NetCDF writer and reader on the
     workload's files: the density model (131,072 cells) and the FTG data of
@@ -568,6 +632,7 @@ def run_batched(args, rank, world, local):
     ctx.close()
     refinement = measure_refinement(s, nmod, args.steps, stream, flush, local, peaks)
     stream_fp32 = measure_stream(args.steps, stream, flush, local, peaks)
+    fp64_configs = measure_fp64_configs(stream, flush, local)
     ftg = data[0].view(n, 10)[:, 1:].reshape(-1).cpu().numpy()
     netcdf_io = measure_netcdf(s, ftg) if rank == 0 else None
     return {
@@ -590,7 +655,8 @@ def run_batched(args, rank, world, local):
         "step": "one CUDA graph per step (batched forward, weighted misfit, batched "
                 "adjoint: %d library kernels + 2 torch kernels), replayed" % launches_per_step,
         "e2e": e2e, "gpu_launches": launches, "roofline": roof, "clocks": clk,
-        "refinement": refinement, "stream_fp32": stream_fp32, "netcdf": netcdf_io,
+        "refinement": refinement, "stream_fp32": stream_fp32, "fp64_configs": fp64_configs,
+        "netcdf": netcdf_io,
     }
 
 

@@ -1,6 +1,6 @@
 """Small, self-contained cases for profiling the kernels with ncu.
 
-    python -m jif3d_gb300.profiling node [--stations 64]   # node-term fwd + adjoint
+    python -m jif3d_gb300.profiling node [--stations 64] [--config 4]  # node-term fwd + adjoint
     python -m jif3d_gb300.profiling fp64-weights           # libm FP64 weight probes
     python -m jif3d_gb300.profiling gemm [--stations 128]  # tensor-core batched products
     python -m jif3d_gb300.profiling stream [--stations 400] # FP32 streaming products
@@ -19,9 +19,13 @@ import sys
 import numpy as np
 
 
-def case_node(stations: int) -> None:
+def case_node(stations: int, config: int = 4) -> None:
+    """Node-term forward and adjoint of one model on a workload's mesh and
+    kind (1 scalar, 2 tensor, 3 or 4 joint, 5 magnetic TFA) with every k-th
+    station, `stations` of them."""
     from . import capi, workloads as W
-    s = W.config4(nmodels=1)
+    s = W.config4(nmodels=1) if config == 4 else W.CONFIGS[config]()
+    s.subsets = None
     step = max(1, s.stations.shape[0] // stations)
     s = s.subset(np.arange(0, s.stations.shape[0], step)[:stations])
     ctx = capi.Context(0)
@@ -134,6 +138,7 @@ def main(argv=None) -> None:
     sub = p.add_subparsers(dest="case", required=True)
     n = sub.add_parser("node")
     n.add_argument("--stations", type=int, default=64)
+    n.add_argument("--config", type=int, default=4, choices=[1, 2, 3, 4, 5])
     w = sub.add_parser("fp64-weights")
     w.add_argument("--iters", type=int, default=1000)
     g = sub.add_parser("gemm")
@@ -147,7 +152,7 @@ def main(argv=None) -> None:
     r.add_argument("--models", type=int, default=32)
     a = p.parse_args(argv)
     if a.case == "node":
-        case_node(a.stations)
+        case_node(a.stations, a.config)
     elif a.case == "gemm":
         case_gemm(a.stations, a.models)
     elif a.case == "stream":
