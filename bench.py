@@ -187,32 +187,37 @@ def timed_steps(step, nsteps, stream, flush):
     return times
 
 
-def host_link(h_in, h_out, stream):
+def host_link(h_in, h_out, load):
     """Host link speed from page-locked buffers (best of 5): the input
-    buffer copied in, the output buffer copied out, and both at once on two
-    streams (GB/s of all bytes moved)."""
+    buffer copied in, the output buffer copied out, both at once on two
+    streams, and both at once while `load` (device steps queued on the
+    compute stream, longer than the copies) runs (GB/s of all bytes moved)."""
     import torch
     d_in = torch.empty_like(h_in, device="cuda")
     d_out = torch.empty_like(h_out, device="cuda")
-    s2 = torch.cuda.Stream()
+    s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
     nb_in, nb_out = h_in.numel() * 8, h_out.numel() * 8
 
-    def best(fn, nbytes):
+    def best(fn, nbytes, busy=None):
         t = []
         for _ in range(5):
             torch.cuda.synchronize()
+            if busy:
+                busy()
             t0 = time.perf_counter()
             fn()
-            torch.cuda.synchronize()
+            s_in.synchronize()
+            s_out.synchronize()
             t.append(time.perf_counter() - t0)
+            torch.cuda.synchronize()
         return nbytes / min(t) / 1e9
 
     def h2d():
-        with torch.cuda.stream(stream):
+        with torch.cuda.stream(s_in):
             d_in.copy_(h_in, non_blocking=True)
 
     def d2h():
-        with torch.cuda.stream(s2):
+        with torch.cuda.stream(s_out):
             h_out.copy_(d_out, non_blocking=True)
 
     def both():
@@ -220,8 +225,10 @@ def host_link(h_in, h_out, stream):
         d2h()
     r = {"h2d_gbs": best(h2d, nb_in), "d2h_gbs": best(d2h, nb_out),
          "both_gbs": best(both, nb_in + nb_out),
+         "both_under_load_gbs": best(both, nb_in + nb_out, load),
          "how": "torch copies of the pinned step buffers (models in, gradients out), "
-                "alone and on two streams at once; best of 5"}
+                "alone and on two streams at once, idle and with three batched steps "
+                "queued on the compute stream; best of 5"}
     del d_in, d_out
     return r
 
@@ -549,14 +556,14 @@ def run_batched(args, rank, world, local):
         sets.append(st)
     obs_t, w_t = d_obs.cpu(), torch.from_numpy(1.0 / sig ** 2)
 
-    def misfit(st):
+    def host_misfit(st):
         torch.mul(torch.sub(st["data"], obs_t, out=st["mis"]), w_t, out=st["mis"])
 
     def e2e_blocking(nsteps):
         st = sets[0]
         for _ in range(nsteps):
             ctx.batched_forward(st["models"].numpy(), out=st["data"].numpy())
-            misfit(st)
+            host_misfit(st)
             ctx.batched_lqderivative(st["models"].numpy(), st["mis"].numpy(),
                                      out=st["grads"].numpy())
 
@@ -576,7 +583,7 @@ def run_batched(args, rank, world, local):
         for i in range(nsteps):
             st = sets[i % 2]
             ctx.batched_wait(fwd[i])
-            misfit(st)
+            host_misfit(st)
             adj[i] = ctx.batched_lqderivative_async(st["models"].numpy(), st["mis"].numpy(),
                                                     out=st["grads"].numpy())
             if i + 2 < nsteps:
@@ -597,8 +604,13 @@ def run_batched(args, rank, world, local):
     e2e_s = max_over_ranks(t2 - t1, world)
     nbytes_in = 8 * (s.models.size + data.numel())
     nbytes_out = 8 * (data.numel() + s.models.size)
-    link = host_link(sets[0]["models"], sets[1]["grads"], stream)
+    def load():
+        for _ in range(3):
+            step()
+    link = host_link(sets[0]["models"], sets[1]["grads"], load)
     link["bound_ms_per_step"] = (nbytes_in + nbytes_out) / (link["both_gbs"] * 1e6)
+    link["bound_under_load_ms_per_step"] = ((nbytes_in + nbytes_out) /
+                                            (link["both_under_load_gbs"] * 1e6))
     e2e = {"value": units * world * args.steps / e2e_s / 1e6, "unit": UNIT,
            "h2d_bytes_per_step": nbytes_in, "host_buffers": "pinned",
            "d2h_bytes_per_step": nbytes_out, "ms_per_step": e2e_s * 1e3 / args.steps,
