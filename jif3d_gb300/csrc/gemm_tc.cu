@@ -175,6 +175,15 @@ __device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t *v) {
       : "r"(taddr));
 }
 
+// s0 += a0 and s1 += a1 as one paired FP32 instruction (add.rn.f32x2,
+// sm_100 and later): two round-to-nearest IEEE adds in half the issue slots.
+__device__ __forceinline__ void fadd2_rn(float &s0, float &s1, uint32_t a0, uint32_t a1) {
+  asm("{\n .reg .b64 x, y;\n mov.b64 x, {%0, %1};\n mov.b64 y, {%2, %3};\n"
+      " add.rn.f32x2 x, x, y;\n mov.b64 {%0, %1}, x;\n}"
+      : "+f"(s0), "+f"(s1)
+      : "r"(a0), "r"(a1));
+}
+
 // Register dependence on 16 loaded values: uses of v stay after this point.
 __device__ __forceinline__ void reg_fence16(uint32_t *v) {
   asm volatile(""
@@ -668,8 +677,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads, 1)
 #pragma unroll
         for (int h = 0; h < kPairLoads; ++h) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j)
-            s[16 * (h0 + h) + j] = __fadd_rn(s[16 * (h0 + h) + j], __uint_as_float(v[h][j]));
+          for (int j = 0; j < 16; j += 2)
+            fadd2_rn(s[16 * (h0 + h) + j], s[16 * (h0 + h) + j + 1], v[h][j], v[h][j + 1]);
         }
       }
       tc_fence_before();
