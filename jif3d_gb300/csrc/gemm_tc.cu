@@ -400,12 +400,18 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 //   empty[s]   both CTAs: stage s free (MMA commit, multicast to the pair)
 //   a_full[b]  both CTAs: accumulator b ready (MMA commit, multicast)
 //   a_empty[b] even CTA only: accumulator b drained in both CTAs (one arrival
-//              per CTA after its 8 drain warps meet at a named barrier)
+//              per CTA after its 16 drain warps meet at a named barrier)
 //   done       even CTA only: every issued MMA finished
 // Waits are bounded as in k_gemm_x3; on expiry a CTA records an error code,
 // stops issuing and runs on to the closing cluster barrier, which both CTAs
 // always reach before the TMEM is freed.
 constexpr int kPairN = 256;   // N of the tile (and of each MMA)
+// Drain warps: four per TMEM lane quarter, each summing 64 of the 256
+// accumulator columns (64 FP32 sums and one 16-column load in flight fit the
+// 112 registers a thread gets at 576 threads).
+constexpr int kPairDrainWarps = 16;
+constexpr int kPairThreads = 64 + 32 * kPairDrainWarps;  // TMA warp, MMA warp, drain warps
+static_assert(kPairDrainWarps * 32 == 512, "the named barriers count 512 drain threads");
 constexpr int kPairAcc = 2;   // accumulators of 256 columns: all 512 TMEM columns
 constexpr int kPairLoads = 1; // TMEM loads (16 columns each) in flight per wait
 
@@ -421,7 +427,7 @@ template <bool F16> struct PairCfg {
   // M = 256 across the pair, N = 256
   static constexpr uint32_t IDESC = (1u << 4) | (FMT << 7) | (FMT << 10) |
                                     ((uint32_t)(kPairN >> 3) << 17) | ((uint32_t)(256 >> 4) << 24);
-  static constexpr int COLS_PER_WARP = kPairN / 2;
+  static constexpr int COLS_PER_WARP = kPairN / (kPairDrainWarps / 4);
 };
 
 __device__ __forceinline__ uint32_t cluster_rank() {
@@ -451,19 +457,19 @@ __device__ __forceinline__ void mbar_arrive_remote(uint32_t cluster_bar) {
                : "memory");
 }
 
-// Named barrier 1 over the 8 drain warps (256 threads): AND of a predicate,
-// and a plain rendezvous.
+// Named barrier 1 over the pair kernel's 16 drain warps (512 threads): AND of
+// a predicate, and a plain rendezvous.
 __device__ __forceinline__ bool drain_all(bool v) {
   uint32_t r;
   asm volatile(
-      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.and.pred p, 1, 256, q;\n"
+      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.and.pred p, 1, 512, q;\n"
       " selp.u32 %0, 1, 0, p;\n}"
       : "=r"(r)
       : "r"((uint32_t)v)
       : "memory");
   return r != 0;
 }
-__device__ __forceinline__ void drain_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+__device__ __forceinline__ void drain_sync() { asm volatile("bar.sync 1, 512;" ::: "memory"); }
 
 // TMA load into this CTA's shared memory that signals an mbarrier of either
 // CTA of the pair (cluster address).
@@ -511,7 +517,7 @@ __device__ __forceinline__ void umma_commit_pair_local(uint32_t bar) {
 }
 
 template <bool F16>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads, 1)
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
     k_gemm_pair(const __grid_constant__ CUtensorMap tmAhi,
                 const __grid_constant__ CUtensorMap tmAlo,
                 const __grid_constant__ CUtensorMap tmBhi,
@@ -651,8 +657,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads, 1)
     }
   } else {
     // ---------------- drain warps (both CTAs) ----------------
-    const int q = warp & 3;
-    const int ch = (warp - 2) >> 2;
+    const int q = warp & 3;          // TMEM lane quarter
+    const int ch = (warp - 2) >> 2;  // column group of COLS_PER_WARP
     const uint32_t lane_off = (uint32_t)(q * 32) << 16;
     const uint32_t col0 = (uint32_t)(ch * C::COLS_PER_WARP);
     float s[C::COLS_PER_WARP];
@@ -660,7 +666,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kGemmThreads, 1)
     for (int j = 0; j < C::COLS_PER_WARP; ++j) s[j] = 0.0f;
     for (int d = 0; d < ndrain; ++d) {
       const int b = d % kPairAcc;
-      // the 8 drain warps decide together, so none is left at the rendezvous
+      // the drain warps decide together, so none is left at the rendezvous
       const bool got = drain_all(mbar_wait(smem_u32(a_full + b), (uint32_t)(d / kPairAcc) & 1u));
       if (!got) {
         if (warp == 2 && lane == 0) atomicExch(err, 4);
@@ -816,7 +822,7 @@ cudaError_t launch_pair(const GemmOperands &g, int nsplit, float *P, long long l
   if (e != cudaSuccess) return e;
   // x: CTA pairs over M (two CTAs of 128 rows each), y: N tiles of 256, z: K splits
   dim3 grid((unsigned)(2 * ((g.m + 255) / 256)), (unsigned)(g.n_pad / kPairN), (unsigned)nsp);
-  k_gemm_pair<F16><<<grid, kGemmThreads, PairCfg<F16>::SMEM, st>>>(
+  k_gemm_pair<F16><<<grid, kPairThreads, PairCfg<F16>::SMEM, st>>>(
       ah, al, bh, bl, kb_per, kb_total, (int)g.m, (int)g.n, P, ldp, slice, err);
   return cudaGetLastError();
 }
