@@ -399,8 +399,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 //              copies signal it through the pair form of the TMA load)
 //   empty[s]   both CTAs: stage s free (MMA commit, multicast to the pair)
 //   a_full[b]  both CTAs: accumulator b ready (MMA commit, multicast)
-//   a_empty[b] even CTA only: accumulator b drained in both CTAs (one arrival
-//              per CTA after its 16 drain warps meet at a named barrier)
+//   a_empty[b] even CTA only: accumulator b drained in both CTAs (one relaxed
+//              arrival per drain warp of either CTA)
 //   done       even CTA only: every issued MMA finished
 // Waits are bounded as in k_gemm_x3; on expiry a CTA records an error code,
 // stops issuing and runs on to the closing cluster barrier, which both CTAs
@@ -411,7 +411,6 @@ constexpr int kPairN = 256;   // N of the tile (and of each MMA)
 // 112 registers a thread gets at 576 threads).
 constexpr int kPairDrainWarps = 16;
 constexpr int kPairThreads = 64 + 32 * kPairDrainWarps;  // TMA warp, MMA warp, drain warps
-static_assert(kPairDrainWarps * 32 == 512, "the named barriers count 512 drain threads");
 constexpr int kPairAcc = 2;   // accumulators of 256 columns: all 512 TMEM columns
 constexpr int kPairLoads = 1; // TMEM loads (16 columns each) in flight per wait
 
@@ -457,19 +456,6 @@ __device__ __forceinline__ void mbar_arrive_remote(uint32_t cluster_bar) {
                : "memory");
 }
 
-// Named barrier 1 over the pair kernel's 16 drain warps (512 threads): AND of
-// a predicate, and a plain rendezvous.
-__device__ __forceinline__ bool drain_all(bool v) {
-  uint32_t r;
-  asm volatile(
-      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.and.pred p, 1, 512, q;\n"
-      " selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(r)
-      : "r"((uint32_t)v)
-      : "memory");
-  return r != 0;
-}
-__device__ __forceinline__ void drain_sync() { asm volatile("bar.sync 1, 512;" ::: "memory"); }
 
 // TMA load into this CTA's shared memory that signals an mbarrier of either
 // CTA of the pair (cluster address).
@@ -548,7 +534,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
     for (int s = 0; s < 2 * S; ++s) mbar_init(smem_u32(bars + s), 1);
     for (int b = 0; b < kPairAcc; ++b) {
       mbar_init(smem_u32(a_full + b), 1);
-      mbar_init(smem_u32(a_empty + b), 2);  // one arrival per CTA
+      mbar_init(smem_u32(a_empty + b), 2 * kPairDrainWarps);  // one per drain warp of the pair
     }
     mbar_init(smem_u32(done), 1);
     *fail = 0;
@@ -666,10 +652,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
     for (int j = 0; j < C::COLS_PER_WARP; ++j) s[j] = 0.0f;
     for (int d = 0; d < ndrain; ++d) {
       const int b = d % kPairAcc;
-      // the drain warps decide together, so none is left at the rendezvous
-      const bool got = drain_all(mbar_wait(smem_u32(a_full + b), (uint32_t)(d / kPairAcc) & 1u));
+      // the lanes decide together: tcgen05.ld below is warp-collective
+      const bool got =
+          __all_sync(0xffffffffu, mbar_wait(smem_u32(a_full + b), (uint32_t)(d / kPairAcc) & 1u));
       if (!got) {
-        if (warp == 2 && lane == 0) atomicExch(err, 4);
+        if (lane == 0) atomicExch(err, 4);
         break;
       }
       tc_fence_after();
@@ -688,9 +675,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
         }
       }
       tc_fence_before();
-      drain_sync();
-      // accumulator b is reused by drain d + kPairAcc: one arrival per CTA
-      if (warp == 2 && lane == 0 && d + kPairAcc < ndrain) {
+      __syncwarp();
+      // accumulator b is reused by drain d + kPairAcc: one relaxed arrival per
+      // drain warp once its loads are complete (no named barrier per drain)
+      if (lane == 0 && d + kPairAcc < ndrain) {
         if (rank == 0)
           mbar_arrive(smem_u32(a_empty + b));
         else
