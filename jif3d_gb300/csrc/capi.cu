@@ -842,7 +842,7 @@ int batched_forward_pass(j3g_context *c, int nmod, const double *d_models, doubl
       J3G_LAUNCH(c, launch_split_matrix(d_models, np, nmod, K, nullptr, c->Bhi.p, c->Blo.p, ldK,
                                         (int)npad, ptr<float>(c->mscale), ptr<double>(c->mmean),
                                         ptr<double>(c->swork), c->stream));
-      c->launches += 2;  // statistics, finalise and split passes
+      c->launches += split_matrix_launches(true, ldK) - 1;
     }
     const long long slice = (long long)nmod * R;
     GemmOperands g{c->Jhi.p, c->Jlo.p, R, c->Bhi.p, c->Blo.p, nmod, npad, ldK, true};
@@ -924,7 +924,7 @@ int batched_adjoint_pass(j3g_context *c, int nmod, const double *d_models,
       J3G_LAUNCH(c, launch_split_matrix(ptr<double>(c->wst), R, nmod, R, ptr<float>(c->rowscale),
                                         c->Bhi.p, c->Blo.p, ldR, (int)npad, ptr<float>(c->mscale),
                                         nullptr, ptr<double>(c->swork), c->stream));
-      c->launches += 2;  // statistics, finalise and split passes
+      c->launches += split_matrix_launches(false, ldR) - 1;
     }
     const long long slice = (long long)nmod * K;
     GemmOperands g{c->JThi.p, c->JTlo.p, K, c->Bhi.p, c->Blo.p, nmod, npad, ldR, true};

@@ -143,13 +143,16 @@ __global__ void k_transpose16(const uint16_t *__restrict__ in, long long ld_in, 
 }
 
 // Splitting an FP64 matrix [nrow][ld_src] (rows = models or residual vectors)
-// into fp16 hi / lo rows [nrow_pad][ld_dst], in three grid-wide passes so that
+// into fp16 hi / lo rows [nrow_pad][ld_dst], in two grid-wide passes so that
 // a few hundred long rows still fill the GPU:
 //   k_row_stats     per (row, column chunk): max |v| and sum v
-//   k_row_finalize  per row: power-of-two scale, optional mean (centring)
-//   k_split_chunks  per (row, column chunk): (v - mean) / scale -> hi + lo
+//   k_split_chunks  per (row, column chunk): the row's power-of-two scale and
+//                   optional mean (centring) from the partials, then
+//                   (v - mean) / scale -> hi + lo
+// Short rows without centring go in one pass (k_split_rows_small).
 // v = src[r][c] * colscale[c] (colscale optional).
 constexpr int kChunk = 8192;
+constexpr long long kSmallRow = 16384;  // rows up to this length split in one pass
 constexpr int kBatch = 8;  // loads in flight per thread in the streaming passes
 static_assert(kChunk % (kT * kBatch) == 0, "chunk must be whole load batches");
 // Column chunk of a split: kChunk, or one load batch per thread (kT * kBatch)
@@ -205,32 +208,48 @@ __global__ void k_row_stats(const double *__restrict__ src, long long ld_src, in
   if (threadIdx.x == 0) part_sum[r * nchunk + blockIdx.x] = sum;
 }
 
-__global__ void k_row_finalize(int nrow_pad, int nchunk, long long ncol, bool center,
-                               const double *__restrict__ part_max,
-                               const double *__restrict__ part_sum, float *__restrict__ rowscale,
-                               double *__restrict__ rowmean) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrow_pad) return;
+// Scale (and mean) of row r from its chunks' partial maxima and sums, in
+// chunk order -- the finalize step, evaluated alike by every block of the row.
+__device__ __forceinline__ void row_scale_mean(int r, int nchunk, long long ncol, bool center,
+                                               const double *__restrict__ part_max,
+                                               const double *__restrict__ part_sum,
+                                               float &scale, double &mean) {
   double mx = 0.0, sum = 0.0;
   for (int k = 0; k < nchunk; ++k) {
     mx = fmax(mx, part_max[(long long)r * nchunk + k]);
     sum += part_sum[(long long)r * nchunk + k];
   }
-  const double mean = (center && ncol > 0) ? sum / (double)ncol : 0.0;
+  mean = (center && ncol > 0) ? sum / (double)ncol : 0.0;
   // |v - mean| <= max|v| + |mean| <= 2 max|v|
-  rowscale[r] = (float)pow2_scale(center ? 2.0 * mx : mx);
-  if (rowmean) rowmean[r] = mean;
+  scale = (float)pow2_scale(center ? 2.0 * mx : mx);
 }
 
+// The split of a chunk with the row's scale and mean formed from the
+// statistics pass's partials; the row's first chunk block stores them.
 __global__ void k_split_chunks(const double *__restrict__ src, long long ld_src, int nrow,
-                               long long ncol, const float *__restrict__ colscale,
-                               const float *__restrict__ rowscale,
-                               const double *__restrict__ rowmean, __half *__restrict__ hi,
+                               long long ncol, const float *__restrict__ colscale, int nchunk,
+                               bool center, const double *__restrict__ part_max,
+                               const double *__restrict__ part_sum, float *__restrict__ rowscale,
+                               double *__restrict__ rowmean, __half *__restrict__ hi,
                                __half *__restrict__ lo, long long ld_dst, int chunk) {
   const long long r = blockIdx.y;
   const long long c0 = (long long)blockIdx.x * chunk + threadIdx.x;
-  const double inv = 1.0 / (double)rowscale[r];  // a power of two: exact
-  const double shift = rowmean ? -rowmean[r] * inv : 0.0;
+  __shared__ float sh_scale;
+  __shared__ double sh_mean;
+  if (threadIdx.x == 0) {
+    float sc;
+    double mu;
+    row_scale_mean((int)r, nchunk, ncol, center, part_max, part_sum, sc, mu);
+    sh_scale = sc;
+    sh_mean = mu;
+    if (blockIdx.x == 0) {
+      rowscale[r] = sc;
+      if (rowmean) rowmean[r] = mu;
+    }
+  }
+  __syncthreads();
+  const double inv = 1.0 / (double)sh_scale;  // a power of two: exact
+  const double shift = rowmean ? -sh_mean * inv : 0.0;
   for (int j0 = 0; j0 < chunk / kT; j0 += kBatch) {
     double v[kBatch];
 #pragma unroll
@@ -243,6 +262,55 @@ __global__ void k_split_chunks(const double *__restrict__ src, long long ld_src,
       // one FP64 operation per element, (v - mean) / scale; then FP32: the
       // 24-bit float keeps more than the 22 bits that hi + lo carry
       const float x = (r < nrow && c < ncol) ? f64_to_f32_ftz(fma(v[u], inv, shift)) : 0.0f;
+      const __half hv = __float2half_rn(x);
+      hi[r * ld_dst + c] = hv;
+      lo[r * ld_dst + c] = __float2half_rn(__fsub_rn(x, __half2float(hv)));
+    }
+  }
+}
+
+// Rows without centring that a block covers alone (the scaled residuals of
+// the adjoint): max |v|, the power-of-two scale and the split in one launch,
+// one block per row; the row is read twice (the second time from cache).
+// Same values as the statistics / split passes (a maximum is order-free).
+constexpr int kSmallT = 512;  // threads per row in k_split_rows_small
+__global__ void __launch_bounds__(kSmallT) k_split_rows_small(
+    const double *__restrict__ src, long long ld_src, int nrow, long long ncol,
+    const float *__restrict__ colscale, float *__restrict__ rowscale, __half *__restrict__ hi,
+    __half *__restrict__ lo, long long ld_dst) {
+  const long long r = blockIdx.x;
+  float mf = 0.0f;
+  for (long long c0 = threadIdx.x; c0 < ld_dst; c0 += (long long)kSmallT * kBatch) {
+    double v[kBatch];  // a batch of independent loads in flight per thread
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u)
+      v[u] = scaled_val(src, ld_src, nrow, ncol, colscale, r, c0 + (long long)u * kSmallT);
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) mf = fmaxf(mf, fabsf(approx_f32(v[u])));
+  }
+  __shared__ double red[kSmallT / 32];
+  __shared__ float sh_scale;
+  double m = warp_max_d((double)mf);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double mm = 0.0;
+    for (int w = 0; w < kSmallT / 32; ++w) mm = fmax(mm, red[w]);
+    sh_scale = (float)pow2_scale(mm);
+    rowscale[r] = sh_scale;
+  }
+  __syncthreads();
+  const double inv = 1.0 / (double)sh_scale;  // a power of two: exact
+  for (long long c0 = threadIdx.x; c0 < ld_dst; c0 += (long long)kSmallT * kBatch) {
+    double v[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u)
+      v[u] = scaled_val(src, ld_src, nrow, ncol, colscale, r, c0 + (long long)u * kSmallT);
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const long long c = c0 + (long long)u * kSmallT;
+      if (c >= ld_dst) break;
+      const float x = (r < nrow && c < ncol) ? f64_to_f32_ftz(fma(v[u], inv, 0.0)) : 0.0f;
       const __half hv = __float2half_rn(x);
       hi[r * ld_dst + c] = hv;
       lo[r * ld_dst + c] = __float2half_rn(__fsub_rn(x, __half2float(hv)));
@@ -665,6 +733,10 @@ cudaError_t launch_transpose16(const void *in, long long ld_in, long long rows, 
   return cudaGetLastError();
 }
 
+int split_matrix_launches(bool center, long long ld_dst) {
+  return (!center && ld_dst <= kSmallRow) ? 1 : 2;
+}
+
 long long split_matrix_work(int nrow_pad, long long ld_dst) {
   const long long chunk = split_chunk(nrow_pad, ld_dst);
   return 2LL * nrow_pad * ((ld_dst + chunk - 1) / chunk);
@@ -677,16 +749,19 @@ cudaError_t launch_split_matrix(const double *src, long long ld_src, int nrow, l
   if (nrow_pad == 0) return cudaSuccess;
   const int chunk = (int)split_chunk(nrow_pad, ld_dst);
   const int nchunk = cdiv(ld_dst, chunk);
+  if (!rowmean && ld_dst <= kSmallRow) {
+    k_split_rows_small<<<nrow_pad, kSmallT, 0, st>>>(src, ld_src, nrow, ncol, colscale, rowscale,
+                                                static_cast<__half *>(hi),
+                                                static_cast<__half *>(lo), ld_dst);
+    return cudaGetLastError();
+  }
   double *pmax = work, *psum = work + (long long)nrow_pad * nchunk;
   dim3 grid(nchunk, nrow_pad);
   k_row_stats<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, pmax, psum, nchunk, chunk);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_row_finalize<<<cdiv(nrow_pad, 128), 128, 0, st>>>(nrow_pad, nchunk, ncol, rowmean != nullptr,
-                                                      pmax, psum, rowscale, rowmean);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  k_split_chunks<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, rowscale, rowmean,
+  k_split_chunks<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, nchunk,
+                                      rowmean != nullptr, pmax, psum, rowscale, rowmean,
                                       static_cast<__half *>(hi), static_cast<__half *>(lo),
                                       ld_dst, chunk);
   return cudaGetLastError();
