@@ -143,12 +143,11 @@ __global__ void k_transpose16(const uint16_t *__restrict__ in, long long ld_in, 
 }
 
 // Splitting an FP64 matrix [nrow][ld_src] (rows = models or residual vectors)
-// into fp16 hi / lo rows [nrow_pad][ld_dst], in two grid-wide passes so that
+// into fp16 hi / lo rows [nrow_pad][ld_dst], in three grid-wide passes so that
 // a few hundred long rows still fill the GPU:
 //   k_row_stats     per (row, column chunk): max |v| and sum v
-//   k_split_chunks  per (row, column chunk): the row's power-of-two scale and
-//                   optional mean (centring) from the partials, then
-//                   (v - mean) / scale -> hi + lo
+//   k_row_finalize  per row: power-of-two scale, optional mean (centring)
+//   k_split_chunks  per (row, column chunk): (v - mean) / scale -> hi + lo
 // Short rows without centring go in one pass (k_split_rows_small).
 // v = src[r][c] * colscale[c] (colscale optional).
 constexpr int kChunk = 8192;
@@ -208,48 +207,32 @@ __global__ void k_row_stats(const double *__restrict__ src, long long ld_src, in
   if (threadIdx.x == 0) part_sum[r * nchunk + blockIdx.x] = sum;
 }
 
-// Scale (and mean) of row r from its chunks' partial maxima and sums, in
-// chunk order -- the finalize step, evaluated alike by every block of the row.
-__device__ __forceinline__ void row_scale_mean(int r, int nchunk, long long ncol, bool center,
-                                               const double *__restrict__ part_max,
-                                               const double *__restrict__ part_sum,
-                                               float &scale, double &mean) {
+__global__ void k_row_finalize(int nrow_pad, int nchunk, long long ncol, bool center,
+                               const double *__restrict__ part_max,
+                               const double *__restrict__ part_sum, float *__restrict__ rowscale,
+                               double *__restrict__ rowmean) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrow_pad) return;
   double mx = 0.0, sum = 0.0;
   for (int k = 0; k < nchunk; ++k) {
     mx = fmax(mx, part_max[(long long)r * nchunk + k]);
     sum += part_sum[(long long)r * nchunk + k];
   }
-  mean = (center && ncol > 0) ? sum / (double)ncol : 0.0;
+  const double mean = (center && ncol > 0) ? sum / (double)ncol : 0.0;
   // |v - mean| <= max|v| + |mean| <= 2 max|v|
-  scale = (float)pow2_scale(center ? 2.0 * mx : mx);
+  rowscale[r] = (float)pow2_scale(center ? 2.0 * mx : mx);
+  if (rowmean) rowmean[r] = mean;
 }
 
-// The split of a chunk with the row's scale and mean formed from the
-// statistics pass's partials; the row's first chunk block stores them.
 __global__ void k_split_chunks(const double *__restrict__ src, long long ld_src, int nrow,
-                               long long ncol, const float *__restrict__ colscale, int nchunk,
-                               bool center, const double *__restrict__ part_max,
-                               const double *__restrict__ part_sum, float *__restrict__ rowscale,
-                               double *__restrict__ rowmean, __half *__restrict__ hi,
+                               long long ncol, const float *__restrict__ colscale,
+                               const float *__restrict__ rowscale,
+                               const double *__restrict__ rowmean, __half *__restrict__ hi,
                                __half *__restrict__ lo, long long ld_dst, int chunk) {
   const long long r = blockIdx.y;
   const long long c0 = (long long)blockIdx.x * chunk + threadIdx.x;
-  __shared__ float sh_scale;
-  __shared__ double sh_mean;
-  if (threadIdx.x == 0) {
-    float sc;
-    double mu;
-    row_scale_mean((int)r, nchunk, ncol, center, part_max, part_sum, sc, mu);
-    sh_scale = sc;
-    sh_mean = mu;
-    if (blockIdx.x == 0) {
-      rowscale[r] = sc;
-      if (rowmean) rowmean[r] = mu;
-    }
-  }
-  __syncthreads();
-  const double inv = 1.0 / (double)sh_scale;  // a power of two: exact
-  const double shift = rowmean ? -sh_mean * inv : 0.0;
+  const double inv = 1.0 / (double)rowscale[r];  // a power of two: exact
+  const double shift = rowmean ? -rowmean[r] * inv : 0.0;
   for (int j0 = 0; j0 < chunk / kT; j0 += kBatch) {
     double v[kBatch];
 #pragma unroll
@@ -734,7 +717,7 @@ cudaError_t launch_transpose16(const void *in, long long ld_in, long long rows, 
 }
 
 int split_matrix_launches(bool center, long long ld_dst) {
-  return (!center && ld_dst <= kSmallRow) ? 1 : 2;
+  return (!center && ld_dst <= kSmallRow) ? 1 : 3;
 }
 
 long long split_matrix_work(int nrow_pad, long long ld_dst) {
@@ -760,8 +743,11 @@ cudaError_t launch_split_matrix(const double *src, long long ld_src, int nrow, l
   k_row_stats<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, pmax, psum, nchunk, chunk);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_split_chunks<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, nchunk,
-                                      rowmean != nullptr, pmax, psum, rowscale, rowmean,
+  k_row_finalize<<<cdiv(nrow_pad, 128), 128, 0, st>>>(nrow_pad, nchunk, ncol, rowmean != nullptr,
+                                                      pmax, psum, rowscale, rowmean);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_split_chunks<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, rowscale, rowmean,
                                       static_cast<__half *>(hi), static_cast<__half *>(lo),
                                       ld_dst, chunk);
   return cudaGetLastError();

@@ -37,7 +37,7 @@ cudaError_t launch_transpose16(const void *in, long long ld_in, long long rows, 
 // the ncol columns).  work: split_matrix_work(nrow_pad, ld_dst) doubles.
 long long split_matrix_work(int nrow_pad, long long ld_dst);
 // Kernel launches of one launch_split_matrix call (1 for short rows without
-// centring, else 2).
+// centring, else 3).
 int split_matrix_launches(bool center, long long ld_dst);
 cudaError_t launch_split_matrix(const double *src, long long ld_src, int nrow, long long ncol,
                                 const float *colscale, void *hi, void *lo, long long ld_dst,
