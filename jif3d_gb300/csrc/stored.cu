@@ -436,10 +436,11 @@ __global__ void k_splitk_reduce(const float *__restrict__ P, int nsplit, long lo
 // The same over groups of four consecutive rows (nrow, ldp and slice
 // multiples of 4, P 16-byte aligned); grid (row blocks, models), no index
 // division.  A thread takes G groups kT quads apart within one model --
-// consecutive threads read consecutive float4s -- and U splits at a time, so
-// that eight independent 16-byte loads are in flight per thread whatever the
-// number of splits (G = 4 quads x 2 splits for a few splits, 1 quad x 8
-// splits for many, with the next batch loading while one is added up).  The
+// consecutive threads read consecutive float4s -- and U splits at a time:
+// for a few splits G = 2 quads x 2 splits (four loads per thread, twice the
+// threads of four quads: 108 instead of 115 us for the 2-split adjoint of
+// 256 x 131072 outputs), for many 1 quad x 8 splits with the next batch
+// loading while one is added up.  The
 // split sums accumulate as unevaluated FP32 pairs
 // (hi + lo, error-free two-sum), about 48 bits -- as good as an FP64 sum of
 // FP32 partials -- without the FP64 pipe.  With more than kPairSplits splits
@@ -450,7 +451,7 @@ __global__ void k_splitk_reduce(const float *__restrict__ P, int nsplit, long lo
 // power-of-two scales are exponent adds; factor is applied the same way when
 // it is a power of two (fpow2, 2^kfac), else by an FP64 multiply.
 constexpr int kPairSplits = 4;
-// G: row quads per thread (4 for a few splits; 1 for many, so that more
+// G: row quads per thread (2 for a few splits; 1 for many, so that more
 // threads share the splits' loads); U: splits per load batch.  The next
 // batch of loads is issued before the current one is added up.
 template <bool PAIR, int G>  // PAIR: widen hi + lo in FP64 (more than kPairSplits splits)
@@ -796,8 +797,8 @@ cudaError_t launch_splitk_reduce(const float *P, int nsplit, long long slice, in
                                                      modscale, modmean, rowsum, fpow2, kf - 1,
                                                      factor, out, ld_out);
     } else {
-      dim3 grid(cdiv(nrow / 4, (long long)kT * 4), nmod);
-      k_splitk_reduce4<false, 4><<<grid, kT, 0, st>>>(P, nsplit, slice, nrow, ldp, rowscale,
+      dim3 grid(cdiv(nrow / 4, (long long)kT * 2), nmod);
+      k_splitk_reduce4<false, 2><<<grid, kT, 0, st>>>(P, nsplit, slice, nrow, ldp, rowscale,
                                                       modscale, modmean, rowsum, fpow2, kf - 1,
                                                       factor, out, ld_out);
     }
