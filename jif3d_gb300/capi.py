@@ -472,11 +472,15 @@ class Context:
         self._hold(t.value, (m, r, g))
         return t.value
 
+    # calls in flight at once in the library's ring of pipelined calls
+    PIPELINE_SLOTS = 4
+
     def _hold(self, ticket, arrays):
-        """Keep a call's arrays alive until it is waited for; calls three or
-        more tickets older have completed (their ring slot was reused)."""
+        """Keep a call's arrays alive until it is waited for; a call
+        PIPELINE_SLOTS or more tickets older has completed (its ring slot was
+        reused by a later call, which waited for it)."""
         self._inflight[ticket] = arrays
-        for t in [t for t in self._inflight if t <= ticket - 3]:
+        for t in [t for t in self._inflight if t <= ticket - self.PIPELINE_SLOTS]:
             del self._inflight[t]
 
     def batched_wait(self, ticket):

@@ -86,6 +86,9 @@ struct j3g_context {
   // station subsets (j3g_subsets_*): a context over the concatenated subset
   // stations, rebuilt when the subsets or this context's setup change
   long long gen = 0;  // bumped by every set_* call
+  // bumped by everything a captured product depends on beyond its arguments:
+  // set_* calls, buffer (re)allocation, product plans, timing
+  long long prod_gen = 0;
   std::vector<double> hsx, hsy, hsz;
   j3g_context *child = nullptr;
   std::vector<int> child_off, child_idx;
@@ -110,6 +113,14 @@ struct j3g_context {
     cudaEvent_t h2d = nullptr, done = nullptr, d2h = nullptr;
     int *flag = nullptr;    // page-locked copy of the tensor-core error flag
     long long ticket = -1;  // call in flight in this slot, -1 if free
+    // per direction (forward, derivative): the product replayed as a CUDA
+    // graph, valid while prod_gen and the model count are those it was
+    // captured under, and the state of the last eager product
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    long long exec_gen[2] = {-1, -1}, exec_launches[2] = {0, 0};
+    int exec_nmod[2] = {0, 0};
+    long long warm_gen[2] = {-1, -1};
+    int warm_nmod[2] = {0, 0};
   };
   static constexpr int kSlots = 4;
   Slot slots[kSlots];
@@ -195,6 +206,7 @@ int ensure(j3g_context *c, DevBuf &b, size_t bytes) {
     b.cap = 0;
     if (e != cudaSuccess) return cuda_fail(c, e, "cudaFree");
   }
+  ++c->prod_gen;  // captured products hold the old address
   cudaError_t e = cudaMalloc(&b.p, bytes);
   if (e != cudaSuccess) {
     b.p = nullptr;
@@ -804,6 +816,7 @@ int gemm_plan(j3g_context *c, int dir, const GemmOperands &g, long long ldp, lon
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   c->plans[key] = plan;
+  ++c->prod_gen;
   return J3G_OK;
 }
 
@@ -1038,6 +1051,8 @@ int j3g_destroy(j3g_context *c) {
       if (b->p) cudaFree(b->p);
     for (cudaEvent_t e : {sl.h2d, sl.done, sl.d2h})
       if (e) cudaEventDestroy(e);
+    for (cudaGraphExec_t g : sl.exec)
+      if (g) cudaGraphExecDestroy(g);
     if (sl.flag) cudaFreeHost(sl.flag);
   }
   if (c->h2d_stream) cudaStreamDestroy(c->h2d_stream);
@@ -1106,6 +1121,7 @@ int j3g_set_mesh(j3g_context *c, int nx, int ny, int nz, const double *xc, const
   c->bg_dirty = true;
   drop_stored(c);  // the stored sensitivity belongs to the old geometry
   ++c->gen;
+  ++c->prod_gen;
   return J3G_OK;
 }
 
@@ -1119,6 +1135,7 @@ int j3g_set_background(j3g_context *c, int nbg, const double *thick) {
   c->bg_dirty = true;
   drop_stored(c);  // the stored sensitivity belongs to the old geometry
   ++c->gen;
+  ++c->prod_gen;
   return J3G_OK;
 }
 
@@ -1139,6 +1156,7 @@ int j3g_set_stations(j3g_context *c, int n, const double *x, const double *y, co
   c->bg_dirty = true;
   drop_stored(c);  // the stored sensitivity belongs to the old geometry
   ++c->gen;
+  ++c->prod_gen;
   return J3G_OK;
 }
 
@@ -1158,6 +1176,7 @@ int j3g_set_kind(j3g_context *c, int kind, double inc, double dec, double fs) {
     if (!ok) c->transform = J3G_T_NONE;
   }
   ++c->gen;
+  ++c->prod_gen;
   return J3G_OK;
 }
 
@@ -1174,6 +1193,7 @@ int j3g_set_transform(j3g_context *c, int transform, double inc, double dec) {
   c->tinc = inc;
   c->tdec = dec;
   ++c->gen;
+  ++c->prod_gen;
   return J3G_OK;
 }
 
@@ -1430,9 +1450,57 @@ struct PipeCopy {
   DevBuf *dev;
   size_t n;
 };
-int pipeline_run(j3g_context *c, j3g_context::Slot *slot, std::initializer_list<PipeCopy> ins,
-                 double *h_out, size_t n_out, long long *ticket,
-                 const std::function<int(void)> &product) {
+// The product of a pipelined call on the context's stream: replayed from the
+// slot's CUDA graph when one was captured under the current state, captured
+// when the previous eager product of this shape left the state unchanged (no
+// buffer grew, no plan was tuned), else run eagerly.  With timing on, eager.
+int pipeline_product(j3g_context *c, j3g_context::Slot *slot, int dir, int nmod,
+                     const std::function<int(void)> &product) {
+  if (!c->timing && slot->exec[dir] && slot->exec_gen[dir] == c->prod_gen &&
+      slot->exec_nmod[dir] == nmod) {
+    J3G_CUDA(c, cudaGraphLaunch(slot->exec[dir], c->stream));
+    c->launches += slot->exec_launches[dir];
+    return J3G_OK;
+  }
+  if (!c->timing && slot->warm_gen[dir] == c->prod_gen && slot->warm_nmod[dir] == nmod) {
+    if (slot->exec[dir]) {
+      cudaGraphExecDestroy(slot->exec[dir]);
+      slot->exec[dir] = nullptr;
+    }
+    const long long gen0 = c->prod_gen, l0 = c->launches;
+    J3G_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = product();
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(c->stream, &graph);
+    cudaGraphExec_t exec = nullptr;
+    if (rc == J3G_OK && ec == cudaSuccess && graph && c->prod_gen == gen0 &&
+        cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+      cudaGraphDestroy(graph);
+      slot->exec[dir] = exec;
+      slot->exec_gen[dir] = gen0;
+      slot->exec_nmod[dir] = nmod;
+      slot->exec_launches[dir] = c->launches - l0;
+      J3G_CUDA(c, cudaGraphLaunch(exec, c->stream));
+      return J3G_OK;
+    }
+    // not capturable under this state: nothing ran, run it eagerly
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    c->launches = l0;
+    slot->warm_gen[dir] = -1;
+  }
+  const long long gen0 = c->prod_gen;
+  J3G_TRY(product());
+  if (c->prod_gen == gen0) {
+    slot->warm_gen[dir] = gen0;
+    slot->warm_nmod[dir] = nmod;
+  }
+  return J3G_OK;
+}
+
+int pipeline_run(j3g_context *c, j3g_context::Slot *slot, int dir, int nmod,
+                 std::initializer_list<PipeCopy> ins, double *h_out, size_t n_out,
+                 long long *ticket, const std::function<int(void)> &product) {
   for (const PipeCopy &in : ins) {
     if (!in.host) continue;
     J3G_TRY(ensure(c, *in.dev, sizeof(double) * in.n));
@@ -1442,7 +1510,7 @@ int pipeline_run(j3g_context *c, j3g_context::Slot *slot, std::initializer_list<
   J3G_TRY(ensure(c, slot->out, sizeof(double) * n_out));
   J3G_CUDA(c, cudaEventRecord(slot->h2d, c->h2d_stream));
   J3G_CUDA(c, cudaStreamWaitEvent(c->stream, slot->h2d, 0));
-  J3G_TRY(product());
+  J3G_TRY(pipeline_product(c, slot, dir, nmod, product));
   J3G_CUDA(c, cudaEventRecord(slot->done, c->stream));
   J3G_CUDA(c, cudaStreamWaitEvent(c->d2h_stream, slot->done, 0));
   J3G_CUDA(c, cudaMemcpyAsync(h_out, slot->out.p, sizeof(double) * n_out, cudaMemcpyDeviceToHost,
@@ -1468,7 +1536,8 @@ int j3g_batched_forward_async(j3g_context *c, int nmodels, const double *h_model
   j3g_context::Slot *slot;
   J3G_TRY(pipeline_slot(c, slot));
   const size_t nm = (size_t)nmodels * c->nparm(), nd = (size_t)nmodels * c->nmeas * c->dpm();
-  return pipeline_run(c, slot, {{h_models, &slot->in, nm}}, h_data, nd, ticket, [&]() {
+  return pipeline_run(c, slot, 0, nmodels, {{h_models, &slot->in, nm}}, h_data, nd, ticket,
+                      [&]() {
     return batched_forward_impl(c, nmodels, ptr<double>(slot->in), ptr<double>(slot->out),
                                 nullptr);
   });
@@ -1486,7 +1555,7 @@ int j3g_batched_lqderivative_async(j3g_context *c, int nmodels, const double *h_
   j3g_context::Slot *slot;
   J3G_TRY(pipeline_slot(c, slot));
   const size_t nm = (size_t)nmodels * c->nparm(), nd = (size_t)nmodels * c->nmeas * c->dpm();
-  return pipeline_run(c, slot,
+  return pipeline_run(c, slot, 1, nmodels,
                       {{needs_models ? h_models : nullptr, &slot->in, nm},
                        {h_misfits, &slot->in2, nd}},
                       h_grads, nm, ticket, [&]() {
@@ -1530,6 +1599,7 @@ int j3g_set_timing(j3g_context *c, int enable) {
   cudaStreamSynchronize(c->stream);
   clear_timing(c);
   c->timing = enable != 0;
+  ++c->prod_gen;
   return J3G_OK;
 }
 
@@ -1580,11 +1650,13 @@ int j3g_subsets_lqderivative_device(j3g_context *c, int nsub, const int *h_offse
 int j3g_set_autotune(j3g_context *c, int enable) {
   if (!c) return J3G_ERR_ARG;
   c->autotune = enable != 0;
+  ++c->prod_gen;
   return J3G_OK;
 }
 
 int j3g_set_gemm_plan(j3g_context *c, int direction, int nsplit, int tile) {
   if (!c || direction < 0 || direction > 1) return J3G_ERR_ARG;
+  ++c->prod_gen;
   if (nsplit <= 0) {  // back to the fixed rule / the autotuner
     c->pinned[direction] = false;
     return J3G_OK;

@@ -172,6 +172,55 @@ def test_pipelined_batched_calls(ctx, kind, transform):
         ctx.batched_wait(10 ** 9)
 
 
+def test_pipelined_calls_replay_graphs(ctx):
+    """Pipelined calls replay their products from per-slot CUDA graphs once a
+    shape is warm.  Many calls per slot (eager, captured, replayed), then a
+    pinned plan, another model count and a new geometry -- each of which
+    must retire the graphs -- all give, bit for bit, what the blocking calls
+    give."""
+    import torch
+
+    def pinned(shape):
+        return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+    def run(s, models, mis, ncalls=10):
+        nd = mis.shape[1]
+        outs = [pinned((models.shape[0], nd)) for _ in range(ncalls)]
+        grads = [pinned(models.shape) for _ in range(ncalls)]
+        tf = [ctx.batched_forward_async(models * (1 + 0.01 * k), out=outs[k])
+              for k in range(ncalls)]
+        for t in tf:
+            ctx.batched_wait(t)
+        ta = [ctx.batched_lqderivative_async(None, mis * (k + 1), out=grads[k])
+              for k in range(ncalls)]
+        for t in ta:
+            ctx.batched_wait(t)
+        for k in range(ncalls):
+            assert np.array_equal(outs[k], ctx.batched_forward(models * (1 + 0.01 * k)))
+            assert np.array_equal(grads[k], ctx.batched_lqderivative(models, mis * (k + 1)))
+
+    rng = np.random.default_rng(31)
+    s = small_survey(W.JOINT, seed=291, nx=12, ny=10, nz=8, nmeas=30)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    models = s.model[None, :] * rng.uniform(0.5, 1.5, (260, s.nparm))
+    mis = rng.normal(size=(260, s.stations.shape[0] * 10))
+    run(s, models, mis)
+    try:
+        ctx.set_gemm_plan(0, 6, 256)
+        ctx.set_gemm_plan(1, 3, 128)
+        run(s, models, mis)
+    finally:
+        ctx.set_gemm_plan(0, 0)
+        ctx.set_gemm_plan(1, 0)
+    run(s, models[:70], mis[:70])
+    s2 = small_survey(W.TENSOR, seed=292, nx=9, ny=11, nz=7, nmeas=25)
+    W.setup_context(ctx, s2)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    m2 = s2.model[None, :] * rng.uniform(0.5, 1.5, (200, s2.nparm))
+    run(s2, m2, rng.normal(size=(200, s2.stations.shape[0] * 9)))
+
+
 def test_pinned_gemm_plans(ctx, oracle_lib):
     """Pinned plans (j3g_set_gemm_plan) are used as given -- the CTA pair with
     many K splits, one-SM 128-wide tiles -- and agree with the oracle; a tile
