@@ -252,7 +252,10 @@ int j3g_batched_lqderivative(j3g_context *ctx, int nmodels, const double *h_mode
  * the products of the calls before and after.  j3g_batched_wait(ticket)
  * blocks until that call's output is in host memory.  Up to four calls are
  * in flight (a fifth waits for the first: enough to queue a forward two
- * steps ahead of the misfit it feeds); the host buffers must stay
+ * steps ahead of the misfit it feeds).  A call's product is replayed from a
+ * CUDA graph of its slot once the same shape has run with no buffer grown or
+ * plan tuned; any set_*, plan, timing or sensitivity change retires the
+ * graphs.  The host buffers must stay
  * valid and unchanged until the call is waited for, and page-locked host
  * buffers are needed for the copies to overlap. */
 int j3g_batched_forward_async(j3g_context *ctx, int nmodels, const double *h_models,
