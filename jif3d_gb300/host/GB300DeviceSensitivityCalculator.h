@@ -47,10 +47,12 @@ class GB300DeviceSensitivityCalculator : public ThreeDGravMagCalculator<DataType
   typedef typename DataType::ModelType ModelType;
   typedef GB300GravMagImplementation<DataType> ImpType;
 
-  // storage: J3G_STORE_FP32 (one model at a time at HBM speed) or
-  // J3G_STORE_F16X2 (tensor-core products, the faster choice for batches).
+  // storage: J3G_STORE_FP32 (the default: one copy of J, streamed at HBM
+  // speed, the right choice for one model per call) or J3G_STORE_F16X2
+  // (J and its transpose as fp16 hi / lo, tensor-core products: the faster
+  // choice for CalculateBatch / LQDerivativeBatch over many models).
   explicit GB300DeviceSensitivityCalculator(gb300_detail::shared<ImpType> imp,
-                                            int storage = J3G_STORE_F16X2)
+                                            int storage = J3G_STORE_FP32)
       : ThreeDGravMagCalculator<DataType>(imp), imp_(imp), storage_(storage) {}
 
   virtual rvec Calculate(const ModelType &Model, const DataType &Data) override {
