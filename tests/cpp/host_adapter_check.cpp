@@ -21,7 +21,8 @@
 //   devbatch / devbatchgrad (rows k = 0, 1, 2: the model times 1 + 0.1 k and
 //   the misfit times k + 1), devmoved (station 0 moved by +1 m in x: a new
 //   geometry, FP64 again) and "devexception ok" for a misfit row count that
-//   does not match the models.
+//   does not match the models; dev32cached / dev32grad: the same calculator
+//   with its default FP32 storage.
 #define JIF3D_GB300_STANDALONE
 #include <cstdio>
 #include <fstream>
@@ -172,6 +173,12 @@ void run(const Problem &p, std::shared_ptr<GB300GravMagImplementation<DataType>>
   } catch (const FatalException &) {
     std::fprintf(out, "devexception ok\n");
   }
+  // the default storage (FP32 J) on the original stations
+  GB300DeviceSensitivityCalculator<DataType> dev32(imp);
+  if (auto t = transform_of(p.transform)) dev32.SetDataTransform(t);
+  dev32.Calculate(model, data);  // FP64, builds the FP32 J
+  put(out, "dev32cached", dev32.Calculate(model, data));
+  put(out, "dev32grad", dev32.LQDerivative(model, data, mis));
 }
 
 }  // namespace

@@ -101,3 +101,5 @@ def test_cpp_implementation(oracle_lib, exe, tmp_path, kind, transform):
     moved.stations[0, 0] += 1.0
     assert relerr(o["devmoved"], oracle_forward(oracle_lib, moved)) <= TOL
     assert o.get("devexception")
+    assert relerr(o["dev32cached"], dref) <= TOL_MIXED
+    assert relerr(o["dev32grad"], gref) <= TOL_MIXED
