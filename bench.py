@@ -652,7 +652,8 @@ def run_batched(args, rank, world, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp16x2 (hi+lo) J and models, fp32 accum drained per k-block, fp64 sums",
+        "dtype": "fp16x2 (hi+lo) J and models, fp32 accumulators drained every 32 cells, "
+                 "fp64 split sums",
         "data": "synthetic",
         "config": {"workload": s.name + "_f16x2_256models", "cells": s.ngrid, "stations": n,
                    "models": nmod, "rows": R, "kind": "joint g_z + FTG",

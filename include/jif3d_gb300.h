@@ -231,9 +231,10 @@ int j3g_stored_lqderivative_device(j3g_context *ctx, const double *d_model,
  * misfits like data, gradients like models.  With J3G_STORE_F16X2 storage
  * the products run on the tensor cores: models and scaled misfits are split
  * into fp16 hi / lo parts with power-of-two scales, J M ~= Jhi Mhi + Jhi Mlo
- * + Jlo Mhi; the hi*hi products of each 64-wide k-block are drained from TMEM
- * into FP32 register sums, the cross terms accumulate per K split of at most
- * 4096 cells, and the splits are summed in FP64 (about 1e-7 relative error).
+ * + Jlo Mhi; all three products of every 32 cells go to a fresh TMEM
+ * accumulator (cross terms first), which is drained into FP32 register sums;
+ * K splits of at most 4096 cells are summed as FP32 two-sum pairs and in FP64
+ * (about 1e-7 relative error).
  * The _device forms queue work only; the host forms copy in and out and
  * synchronise (page-locked host buffers copy at full link speed).  The
  * derivative reads the models only under the FTG-invariant and total-field
