@@ -94,6 +94,7 @@ struct j3g_context {
   std::vector<int> child_off, child_idx;
   long long child_gen = -1;
   DevBuf chunks;  // chunk station ranges of a subset adjoint
+  std::vector<int> chunks_h;  // the table now in chunks
   std::map<std::array<long long, 4>, GemmPlan> plans;
   GemmPlan last_plan[2];
 
@@ -487,10 +488,15 @@ int adjoint_device(j3g_context *c, const double *d_model, const double *d_misfit
       first_chunk.push_back((int)starts.size());
       starts.push_back(c->nmeas);
       nchunk = (int)starts.size() - 1;
-      J3G_TRY(ensure(c, c->chunks, sizeof(int) * starts.size()));
-      J3G_CUDA(c, cudaMemcpyAsync(c->chunks.p, starts.data(), sizeof(int) * starts.size(),
-                                  cudaMemcpyHostToDevice, c->stream));
-      J3G_CUDA(c, cudaStreamSynchronize(c->stream));  // the host table is a local
+      // uploaded only when the subsets' chunk layout changes: a repeated call
+      // on the same subsets queues kernels only (and can be graph-captured)
+      if (starts != c->chunks_h) {
+        J3G_TRY(ensure(c, c->chunks, sizeof(int) * starts.size()));
+        J3G_CUDA(c, cudaMemcpyAsync(c->chunks.p, starts.data(), sizeof(int) * starts.size(),
+                                    cudaMemcpyHostToDevice, c->stream));
+        J3G_CUDA(c, cudaStreamSynchronize(c->stream));  // the host table is a local
+        c->chunks_h = starts;
+      }
       d_starts = ptr<int>(c->chunks);
     } else {
       first_chunk = {0, nchunk};

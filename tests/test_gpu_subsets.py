@@ -111,3 +111,54 @@ def test_config5_uneven_subsets(ctx, oracle_lib):
         o += len(sub)
     few = s.subset(subsets[1][:2])
     assert relerr(d[256:258], oracle_forward(oracle_lib, few)) <= TOL
+
+
+def test_uneven_subsets_captured_in_cuda_graph(ctx, oracle_lib):
+    """The uneven-subset forward and adjoint (one launch per direction for
+    all subsets) captured in one CUDA graph after a warm-up call and replayed
+    on a new model written in place: bit for bit the eager calls, and the
+    oracle on each subset."""
+    import torch
+    s = small_survey(W.MAGNETIC, seed=640, nx=10, ny=9, nz=6, nmeas=60, transform=W.T_TFA)
+    rng = np.random.default_rng(41)
+    subsets = [np.sort(rng.choice(60, k, replace=False)) for k in (7, 31, 1, 18, 60)]
+    W.setup_context(ctx, s)
+    total = sum(len(x) for x in subsets)
+    m = dev(s.model)
+    d = torch.zeros(total * s.dpm, dtype=torch.float64, device="cuda")
+    r = dev(rng.normal(size=total * s.dpm))
+    g = torch.zeros((len(subsets), s.nparm), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+
+    def step():
+        ctx.subsets_forward_device(subsets, m.data_ptr(), d.data_ptr())
+        ctx.subsets_lqderivative_device(subsets, m.data_ptr(), r.data_ptr(), g.data_ptr())
+
+    try:
+        with torch.cuda.stream(stream):
+            step()  # warm-up: buffers, background and the chunk table
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream):
+            step()
+        new = s.model * rng.uniform(0.5, 1.5, s.model.size)
+        m.copy_(dev(new))
+        graph.replay()
+        torch.cuda.synchronize()
+        d_graph, g_graph = d.cpu().numpy(), g.cpu().numpy()
+        with torch.cuda.stream(stream):
+            step()
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_stream(None)
+    assert np.array_equal(d_graph, d.cpu().numpy())
+    assert np.array_equal(g_graph, g.cpu().numpy())
+    rr = r.cpu().numpy()
+    o = 0
+    for k, sub in enumerate(subsets):
+        sk = s.subset(sub)
+        n = len(sub)
+        assert relerr(d_graph[o:o + n], oracle_forward(oracle_lib, sk, new)) <= TOL
+        assert relerr(g_graph[k], oracle_lqderivative(oracle_lib, sk, rr[o:o + n], new)) <= TOL
+        o += n
