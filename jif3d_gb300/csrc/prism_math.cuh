@@ -59,8 +59,17 @@ inline double add(double a, double b) { return a + b; }
 inline double sub(double a, double b) { return a - b; }
 #endif
 
+// v < kEps on the integer pipe (the FP64 pipe is this kernel family's
+// bound): negative values (sign bit set, -0 and -inf included) are below, a
+// NaN of either sign is not, and non-negative doubles order as their bits.
+__device__ __forceinline__ bool lt_eps(double v) {
+  const long long b = __double_as_longlong(v);
+  constexpr long long kEpsBits = 0x3cb0000000000000ll;  // 2^-52
+  return b < 0 ? (b & 0x7fffffffffffffffll) <= 0x7ff0000000000000ll : b < kEpsBits;
+}
+
 // Clamp from below that keeps NaN, like std::max(v, eps).
-__device__ __forceinline__ double clamp_eps(double v) { return (v < kEps) ? kEps : v; }
+__device__ __forceinline__ double clamp_eps(double v) { return lt_eps(v) ? kEps : v; }
 
 // All node terms needed by `mask` (bit c set -> component c) for one offset
 // (dx, dy, dz) = station - node.  One square root serves every component.
@@ -79,7 +88,7 @@ __device__ __forceinline__ void node_terms(double dx, double dy, double dz, doub
     ly = flog(add(dy, rg));
     if (need_gz) {
       double a;
-      if ((MASK & (1 << NC_ZZ)) && !(r < kEps)) {
+      if ((MASK & (1 << NC_ZZ)) && !lt_eps(r)) {
         // g_z's atan2(dz r, dx dy) and Uzz's atan2(dx dy, dz r) share their ratio
         double zz;
         fatan2_pair(mul(dz, rg), mul(dx, dy), a, zz);
@@ -91,15 +100,15 @@ __device__ __forceinline__ void node_terms(double dx, double dy, double dz, doub
       out[NC_GZ] = add(add(mul(dx, ly), mul(dy, lx)), mul(dz, a));
     }
     if (need_off) {
-      const bool shared = !(r < kEps);
+      const bool shared = !lt_eps(r);
       const double ax = add(dx, r), ay = add(dy, r), az = add(dz, r);
       const double log_eps = fp64tab::kLogDblEps;  // log(DBL_EPSILON)
       if (MASK & (1 << NC_YZ))
-        out[NC_YZ] = (ax < kEps) ? log_eps : (shared ? lx : flog(ax));
+        out[NC_YZ] = lt_eps(ax) ? log_eps : (shared ? lx : flog(ax));
       if (MASK & (1 << NC_XZ))
-        out[NC_XZ] = (ay < kEps) ? log_eps : (shared ? ly : flog(ay));
+        out[NC_XZ] = lt_eps(ay) ? log_eps : (shared ? ly : flog(ay));
       if (MASK & (1 << NC_XY))
-        out[NC_XY] = (az < kEps) ? log_eps : flog(az);
+        out[NC_XY] = lt_eps(az) ? log_eps : flog(az);
     }
   }
   if (MASK & (1 << NC_XX)) out[NC_XX] = fatan2(mul(dy, dz), mul(dx, r));
