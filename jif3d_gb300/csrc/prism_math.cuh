@@ -75,7 +75,9 @@ __device__ __forceinline__ double clamp_eps(double v) { return lt_eps(v) ? kEps 
 // (dx, dy, dz) = station - node.  One square root serves every component.
 template <int MASK>
 __device__ __forceinline__ void node_terms(double dx, double dy, double dz, double *out) {
-  const double s2 = add(add(mul(dx, dx), mul(dy, dy)), mul(dz, dz));
+  // fused: the node terms need r to FP64 accuracy, not the reference's
+  // rounding (the eight-corner path keeps that)
+  const double s2 = __fma_rn(dx, dx, __fma_rn(dy, dy, mul(dz, dz)));
   const double r = sqrt(s2);
   constexpr bool need_gz = MASK & (1 << NC_GZ);
   constexpr bool need_off = MASK & ((1 << NC_XY) | (1 << NC_XZ) | (1 << NC_YZ));
@@ -97,7 +99,7 @@ __device__ __forceinline__ void node_terms(double dx, double dy, double dz, doub
         a = fatan2(mul(dz, rg), mul(dx, dy));
         if (MASK & (1 << NC_ZZ)) out[NC_ZZ] = fatan2(mul(dx, dy), mul(dz, r));
       }
-      out[NC_GZ] = add(add(mul(dx, ly), mul(dy, lx)), mul(dz, a));
+      out[NC_GZ] = __fma_rn(dx, ly, __fma_rn(dy, lx, mul(dz, a)));
     }
     if (need_off) {
       const bool shared = !lt_eps(r);
