@@ -7,7 +7,7 @@
 //   flog    -- P. T. P. Tang's table-driven logarithm (ACM TOMS 16(4), 1990):
 //              x = 2^k m, m near F_j = 1 + j/128, u = (m - F_j)/F_j,
 //              log x = k ln2 + log F_j + log1p(u), log1p by its Taylor series
-//              to u^7 (|u| <= 2^-8); 14 FP64 operations.
+//              to u^7 (|u| <= 2^-8); 13 FP64 operations.
 //   fatan2  -- t = min(|y|,|x|) / max(|y|,|x|) from an FP32 reciprocal seed
 //              and one Newton step, atan t from the Taylor series of atan
 //              about the nearest breakpoint c_j = j/64 (degree 8,
@@ -58,12 +58,11 @@ __device__ __forceinline__ double flog(double x) {
   q = __fma_rn(u, q, -0.25);
   q = __fma_rn(u, q, 1.0 / 3.0);
   q = __fma_rn(u, q, -0.5);
-  const double p = __dmul_rn(__dmul_rn(u, u), q);
   const double kd = small_int_to_f64((int)e - 1023);
   // k ln2_lead + lead(log F_j) is exact (both are multiples of 2^-42)
   const double hi = __fma_rn(kd, fp64tab::kLn2Lead, __ldg(row + 1));
   double lo = __fma_rn(kd, fp64tab::kLn2Trail, __ldg(row + 2));
-  lo = __dadd_rn(lo, p);
+  lo = __fma_rn(__dmul_rn(u, u), q, lo);  // + u^2 q, rounded once
   lo = __dadd_rn(lo, u);
   return __dadd_rn(hi, lo);
 }
