@@ -358,8 +358,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
 #pragma unroll
       for (int h = 0; h < NV; ++h) {
 #pragma unroll
-        for (int j = 0; j < 16; ++j)
-          s[16 * h + j] = __fadd_rn(s[16 * h + j], __uint_as_float(v[h][j]));
+        for (int j = 0; j < 16; j += 2)
+          fadd2_rn(s[16 * h + j], s[16 * h + j + 1], v[h][j], v[h][j + 1]);
       }
       tc_fence_before();
       __syncwarp();
