@@ -820,6 +820,11 @@ def run_reference(args, rank, world):
     if rank != 0:
         return None
     fn = cpu_cached_products if args.workload == "batched" else cpu_matrix_free
+    # untimed warm-up samples (thread pool, first touch of the rows), then the
+    # timed ones; each sample is bounded to a few seconds of host work
+    nwarm = min(args.warmup, 3)
+    for _ in range(nwarm):
+        fn(budget_s=2.0)
     vals, cores, sample = [], 1, ""
     for _ in range(max(1, min(args.steps, 3))):
         v, cores, sample = fn()
@@ -827,7 +832,7 @@ def run_reference(args, rank, world):
     v = statistics.median(vals)
     return {
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": len(vals),
-        "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "warmup": nwarm, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
         "config": {"workload": "config4_batched_64x64x32_" +
                                ("f16x2_256models" if args.workload == "batched"
