@@ -2,21 +2,33 @@
 """Benchmark of the GB300 prism path: Mcell*station/s of forward + adjoint.
 
 Workloads (synthetic, seeded; jif3d_gb300/workloads.py):
-  batched (default) -- config 4: 64x64x32 cells (50 m, layers 25 m x1.05),
-      32x32 stations at z = -50 m, joint g_z + FTG, 256 density models
-      (Gaussian blobs + N(0, 0.05) g/cm^3).  The sensitivity is built once per
-      geometry from the FP64 box terms and kept in HBM as fp16 hi + lo with a
+  batched (default) -- 64x64x32 cells (50 m, layers 25 m x1.05), 32x32
+      stations at z = -50 m, joint g_z + FTG, 256 density models (Gaussian
+      blobs + N(0, 0.05) g/cm^3).  The sensitivity is built once per geometry
+      from the FP64 box terms and kept in HBM as fp16 hi + lo with a
       power-of-two row scale (as FullSensitivityGravMagCalculator keeps J
-      between calls).  A step = batched forward of the 256 models, the weighted misfit
-      (d - d_obs)/sigma^2, and the batched adjoint 2 J^T r, products on the
-      tensor cores.
+      between calls).  A step = batched forward of the 256 models, the
+      weighted misfit (d - d_obs)/sigma^2, and the batched adjoint 2 J^T r,
+      products on the tensor cores.
   plain -- the FP64 matrix-free forward + adjoint of one model on the same
       survey (box terms recomputed every call).
 
 `value` counts cells x stations x models per second with inputs resident in
 HBM; `e2e` is the same through the C ABI with host buffers (copies inside
-the timed region).  `--impl reference` times the CPU oracle (the C
-restatement of the reference's implementation) on a bounded sample.
+the timed region).  Beside the headline the batched run reports the other
+workloads (g_z 30x30x15, FTG 64x64x32 through the FP32 stored J, joint
+96x96x48, total-field anomaly 128x128x64 over its 32 uneven station subsets),
+each next to the oracle's OpenMP forward and adjoint on the host cores.
+`--impl reference` times the CPU oracle (the C restatement of the reference's
+implementation) on a bounded sample.
+
+`--case` runs one small, self-contained case of a kernel family and exits
+(for profiler captures that must end by themselves):
+  node    -- FP64 node-term forward + adjoint, `--stations` of `--config`
+  gemm    -- tensor-core batched products, `--stations` of the 64x64x32 survey
+  stream  -- FP32 stored-J products, `--stations` of the FTG survey
+  refine  -- projection / combination to a 2x2x2 refinement, `--models` models
+  batched -- `--steps` batched steps (256 models, all stations), no timing
 """
 from __future__ import annotations
 
@@ -38,11 +50,15 @@ METRIC = "Mcell*station/s fwd+adjoint"
 UNIT = "Mcell*station/s"
 L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
 SIGMA_GZ, SIGMA_U = 1e-8, 1e-9
+# Nominal FP64 (non-tensor) rate of a GB300, for a second FP64 roofline
+# denominator beside the library's own measured FMA rate.
+FP64_NOMINAL_GFLOPS = 1250.0
 
 # FP64 flops per joint node evaluation (an FMA counts 2): 21 add/mul + sqrt +
-# 3 flog + 2 fatan2 + 1 fatan2_pair + 7 accumulation FMA, with the weights
-# measured by ncu on the probe kernels: sqrt 13, flog 21, fatan2 36, pair 42
-# (profiles/fp64_weights.md); the node kernels' own counters give 223 / 214.
+# 3 flog + 2 fatan2 + 1 fatan2_pair + 7 accumulation FMA, with the FP64
+# instruction weights of the device functions counted by ncu on
+# microkernels of each function (sqrt 13, flog 21, fatan2 36, fatan2_pair 42);
+# the node kernels' own counters give 223 (forward) and 214 (adjoint).
 FP64_FLOP_PER_JOINT_NODE = 225.0
 # FP64 flops per node evaluation of the other kinds, counted by ncu
 # (DFMA = 2, DADD, DMUL) on the node kernels, mean of forward and adjoint
@@ -57,6 +73,12 @@ def parse():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--workload", choices=["batched", "plain"], default="batched")
     p.add_argument("--models", type=int, default=256)
+    p.add_argument("--sections", choices=["all", "headline"], default="all",
+                   help="headline: only the batched step and its e2e / roofline (no other "
+                        "workloads, no CPU baselines)")
+    p.add_argument("--case", choices=["node", "gemm", "stream", "refine", "batched"])
+    p.add_argument("--stations", type=int, default=64)
+    p.add_argument("--config", type=int, default=4, choices=[1, 2, 3, 4, 5])
     return p.parse_args()
 
 
@@ -161,11 +183,17 @@ def max_over_ranks(v, world):
     return float(t.item())
 
 
-# DRAM traffic of one tensor-core product launch on config 4 with 256 models,
-# measured with ncu (one-pass dram__bytes_read.sum + dram__bytes_write.sum on
-# the full-size launches of `python -m jif3d_gb300.profiling batched`):
-# forward 3934.5 + 219.2 MB, adjoint 3813.1 + 257.6 MB.
+# DRAM traffic of one tensor-core product launch on the 64x64x32 survey with
+# 1024 stations and 256 models: one-pass dram__bytes_read.sum +
+# dram__bytes_write.sum of the full-size launches, mean of the forward and
+# the adjoint, from the capture
+#   ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum
+#       --clock-control none --csv python bench.py --case batched --steps 2
+# (forward 3934.5 + 219.2 MB, adjoint 3813.1 + 257.6 MB).
 GEMM_DRAM_BYTES_PER_LAUNCH = 0.5 * ((3934.5 + 219.2) + (3813.1 + 257.6)) * 1e6
+GEMM_TRAFFIC_SOURCE = ("ncu one-pass dram__bytes_read.sum + dram__bytes_write.sum of the "
+                       "full-size launches (mean of forward and adjoint) of "
+                       "`python bench.py --case batched --steps 2`, not measured in this run")
 
 
 def sigma_vector(s):
@@ -275,13 +303,44 @@ def measure_refinement(s, nmod, steps, stream, flush, local, peaks):
     return out
 
 
-def measure_stream(steps, stream, flush, local, peaks):
+def cpu_oracle_config(s, nst, seed):
+    """The oracle's OpenMP forward (Calculate) and LQDerivative of one model
+    on the host cores, on `nst` seeded stations of the survey (all of them
+    when it has no more): Mcell*station/s of each and of their sum (the
+    throughput of a (cell, station) pair does not depend on the station)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle import oracle as O
+    from helpers import oracle_forward, oracle_lqderivative
+    O.build()
+    n = s.stations.shape[0]
+    if nst >= n:
+        idx, what = np.arange(n), f"all {n} stations"
+    else:
+        idx = np.sort(np.random.default_rng(seed).choice(n, nst, replace=False))
+        what = f"{nst} of {n} stations (seeded sample, seed {seed})"
+    sub = s.subset(idx)
+    sub.subsets = None
+    misfit = np.random.default_rng(seed + 1).normal(size=idx.size * sub.dpm)
+    t0 = time.perf_counter()
+    oracle_forward(O, sub)
+    t1 = time.perf_counter()
+    oracle_lqderivative(O, sub, misfit)
+    t2 = time.perf_counter()
+    pairs = s.ngrid * idx.size / 1e6
+    return {"value": pairs / (t2 - t0), "forward": pairs / (t1 - t0),
+            "adjoint": pairs / (t2 - t1), "unit": UNIT, "cores": os.cpu_count() or 1,
+            "kind": "port", "seconds": t2 - t0,
+            "sample": f"oracle OpenMP forward + LQDerivative, one model, {what} x all "
+                      f"{s.ngrid} cells"}
+
+
+def measure_stream(steps, stream, flush, local, peaks, cpu):
     """The FTG survey on the 64 x 64 x 32 mesh with 40 x 40 stations: the
     forward and adjoint of one model through the FP32 device-resident J (six
     stored rows per station: 9600 x 131072, 5.03 GB), each streaming J once
     (k_gemv_f32 / k_gemv_t_f32), timed alone with CUDA events, L2 flushed in
-    between; next to the FP64 matrix-free path on the same survey, and the
-    FP32 products' errors against it."""
+    between; next to the FP64 matrix-free path on the same survey, the FP32
+    products' errors against it, and the oracle on the host cores."""
     import torch
     from jif3d_gb300 import capi, workloads as W
     s = W.config2()
@@ -296,11 +355,12 @@ def measure_stream(steps, stream, flush, local, peaks):
     d64, d32 = (torch.zeros(nd, dtype=torch.float64, device=dev) for _ in range(2))
     g64, g32 = (torch.zeros(s.nparm, dtype=torch.float64, device=dev) for _ in range(2))
 
-    def plain():
-        ctx.forward_device(m.data_ptr(), d64.data_ptr())
-        ctx.lqderivative_device(m.data_ptr(), r.data_ptr(), g64.data_ptr())
-    plain()
-    t_plain = statistics.median(timed_steps(plain, 2, stream, flush))
+    fwd64 = lambda: ctx.forward_device(m.data_ptr(), d64.data_ptr())
+    adj64 = lambda: ctx.lqderivative_device(m.data_ptr(), r.data_ptr(), g64.data_ptr())
+    fwd64()
+    adj64()
+    t_pf = statistics.median(timed_steps(fwd64, 2, stream, flush))
+    t_pa = statistics.median(timed_steps(adj64, 2, stream, flush))
     ctx.build_sensitivity(capi.STORE_FP32)
     info = ctx.sensitivity_info()
     fwd = lambda: ctx.stored_forward_device(m.data_ptr(), d32.data_ptr())
@@ -313,13 +373,16 @@ def measure_stream(steps, stream, flush, local, peaks):
     t_a = statistics.median(timed_steps(adj, steps, stream, flush))
     jb = info["bytes"]
     relerr = lambda x, y: float(torch.linalg.norm(x - y) / torch.linalg.norm(y))
+    pairs = s.ngrid * n / 1e6
     out = {"workload": s.name + "_fp32_stored", "cells": s.ngrid, "stations": n,
            "stored_rows": info["rows"], "j_bytes": jb,
-           "value": s.ngrid * n / ((t_f + t_a) * 1e-3) / 1e6, "unit": UNIT,
+           "value": pairs / ((t_f + t_a) * 1e-3), "unit": UNIT,
            "forward_ms": t_f, "adjoint_ms": t_a,
            "forward_gbs": jb / (t_f * 1e-3) / 1e9, "adjoint_gbs": jb / (t_a * 1e-3) / 1e9,
            "hbm_peak_gbs": peaks["hbm_gbs"],
-           "plain_fp64": {"value": s.ngrid * n / (t_plain * 1e-3) / 1e6, "ms_per_step": t_plain},
+           "plain_fp64": {"value": pairs / ((t_pf + t_pa) * 1e-3),
+                          "forward": pairs / (t_pf * 1e-3), "adjoint": pairs / (t_pa * 1e-3),
+                          "ms_per_step": t_pf + t_pa},
            "err_vs_fp64": {"data": relerr(d32, d64), "grad": relerr(g32, g64)},
            "how": "J streamed once per direction (algorithmic bytes = J bytes); times include "
                   "the model conversion, the chunk sums and the assembly / weights kernels"}
@@ -327,23 +390,33 @@ def measure_stream(steps, stream, flush, local, peaks):
     out["adjoint_frac"] = out["adjoint_gbs"] / peaks["hbm_gbs"]
     out["speedup_vs_plain_fp64"] = out["value"] / out["plain_fp64"]["value"]
     ctx.close()
+    if cpu:
+        out["cpu_baseline"] = cpu_oracle_config(s, 64, 202)
+        out["speedup_vs_cpu"] = out["value"] / out["cpu_baseline"]["value"]
+        out["plain_fp64"]["speedup_vs_cpu"] = (out["plain_fp64"]["value"] /
+                                               out["cpu_baseline"]["value"])
     return out
 
 
-def measure_fp64_configs(stream, flush, local):
-    """The FP64 matrix-free forward + adjoint of one model on the other
-    workloads, timed with CUDA events (L2 flushed in between): g_z on the
-    30 x 30 x 15 mesh (400 stations, 3 background layers), joint g_z + FTG on
-    96 x 96 x 48 (2500 stations) and the total-field anomaly on 128 x 128 x 64
-    through the uneven station subsets (the first two of the 32; all 32
-    would take ~45 s).  FP64 roofline: node evaluations x FP64 flops per node
-    of the kind / time against the measured FP64 FMA rate."""
+def measure_fp64_configs(stream, flush, local, cpu):
+    """The FP64 matrix-free forward and adjoint of one model on the other
+    workloads, each timed with CUDA events (L2 flushed in between): g_z on
+    the 30 x 30 x 15 mesh (400 stations, 3 background layers), joint g_z +
+    FTG on 96 x 96 x 48 (2500 stations), and the total-field anomaly on
+    128 x 128 x 64 over all 32 uneven station subsets (74,753 stations in one
+    subsets forward and one subsets adjoint call; no warm-up, one call each,
+    ~40 s).  FP64 roofline: node evaluations x FP64 flops per node of the
+    kind / time, against the library's measured FP64 FMA rate and against the
+    nominal rate.  Beside each, the oracle's OpenMP forward and LQDerivative
+    on the host cores (all stations of the g_z survey, 64 seeded stations of
+    the others)."""
     import torch
     from jif3d_gb300 import capi, workloads as W
     dev = f"cuda:{local}"
     out = {}
     peak = None
-    for cfg, nsub, nsteps in ((1, 0, 5), (3, 0, 2), (5, 2, 1)):
+    for cfg, full_batch, nsteps, cpu_nst in ((1, False, 5, 400), (3, False, 2, 64),
+                                             (5, True, 1, 64)):
         s = W.CONFIGS[cfg]()
         ctx = capi.Context(local)
         ctx.set_stream(stream.cuda_stream)
@@ -351,43 +424,58 @@ def measure_fp64_configs(stream, flush, local):
         peak = peak or ctx.probe_fp64()
         m = torch.tensor(s.model, dtype=torch.float64, device=dev)
         rng = np.random.default_rng(cfg)
-        if nsub:
-            subs = s.subsets[:nsub]
+        if full_batch:
+            subs = s.subsets
             nst = sum(len(x) for x in subs)
             nd = nst * s.dpm
             d = torch.zeros(nd, dtype=torch.float64, device=dev)
             r = torch.tensor(rng.normal(size=nd), dtype=torch.float64, device=dev)
-            g = torch.zeros((nsub, s.nparm), dtype=torch.float64, device=dev)
-
-            def step():
-                ctx.subsets_forward_device(subs, m.data_ptr(), d.data_ptr())
-                ctx.subsets_lqderivative_device(subs, m.data_ptr(), r.data_ptr(), g.data_ptr())
+            g = torch.zeros((len(subs), s.nparm), dtype=torch.float64, device=dev)
+            fwd = lambda: ctx.subsets_forward_device(subs, m.data_ptr(), d.data_ptr())
+            adj = lambda: ctx.subsets_lqderivative_device(subs, m.data_ptr(), r.data_ptr(),
+                                                          g.data_ptr())
         else:
             nst = s.stations.shape[0]
             nd = nst * s.dpm
             d = torch.zeros(nd, dtype=torch.float64, device=dev)
             r = torch.tensor(rng.normal(size=nd), dtype=torch.float64, device=dev)
             g = torch.zeros(s.nparm, dtype=torch.float64, device=dev)
-
-            def step():
-                ctx.forward_device(m.data_ptr(), d.data_ptr())
-                ctx.lqderivative_device(m.data_ptr(), r.data_ptr(), g.data_ptr())
-        step()
-        torch.cuda.synchronize()
-        t = statistics.median(timed_steps(step, nsteps, stream, flush))
+            fwd = lambda: ctx.forward_device(m.data_ptr(), d.data_ptr())
+            adj = lambda: ctx.lqderivative_device(m.data_ptr(), r.data_ptr(), g.data_ptr())
+            fwd()
+            adj()
+            torch.cuda.synchronize()
+        t_f = statistics.median(timed_steps(fwd, nsteps, stream, flush))
+        t_a = statistics.median(timed_steps(adj, nsteps, stream, flush))
+        t = t_f + t_a
         nodes = (s.shape[0] + 1) * (s.shape[1] + 1) * (s.shape[2] + 1)
         kind = s.kind  # scalar 1, tensor 2, magnetic 3, joint 4
         gflops = 2 * nodes * nst * FP64_FLOP_PER_NODE[kind] / (t * 1e-3) / 1e9
-        out[s.name] = {"cells": s.ngrid, "stations": nst, "ms_per_step": t,
-                       "value": s.ngrid * nst / (t * 1e-3) / 1e6, "unit": UNIT,
-                       "fp64_gflops": gflops, "fp64_frac": gflops / peak,
-                       "flop_per_node": FP64_FLOP_PER_NODE[kind]}
-        if nsub:
-            out[s.name]["subsets"] = [len(x) for x in subs]
+        pairs = s.ngrid * nst / 1e6
+        e = {"cells": s.ngrid, "stations": nst, "ms_per_step": t,
+             "forward_ms": t_f, "adjoint_ms": t_a,
+             "value": pairs / (t * 1e-3), "forward": pairs / (t_f * 1e-3),
+             "adjoint": pairs / (t_a * 1e-3), "unit": UNIT,
+             "fp64_gflops": gflops, "fp64_frac": gflops / peak,
+             "fp64_frac_of_nominal": gflops / FP64_NOMINAL_GFLOPS,
+             "flop_per_node": FP64_FLOP_PER_NODE[kind]}
+        if full_batch:
+            e["subsets"] = len(subs)
+            e["subset_sizes"] = [int(min(len(x) for x in subs)), int(max(len(x) for x in subs))]
+            e["how"] = "one subsets forward + one subsets adjoint call over all 32 subsets"
         ctx.close()
+        del d, r, g
+        if cpu:
+            e["cpu_baseline"] = cpu_oracle_config(s, cpu_nst, 200 + cfg)
+            e["speedup_vs_cpu"] = e["value"] / e["cpu_baseline"]["value"]
+        out[s.name] = e
     out["fp64_peak_gflops"] = peak
-    out["how"] = ("forward + adjoint of one model per step; fp64_frac counts node evaluations "
-                  "only (the background, reductions and assembly are in the time)")
+    out["fp64_peak_source"] = ("j3g_probe_fp64: this library's FMA-chain probe kernel "
+                               "(no FP64 figure in MEASURED_PEAKS.json); fp64_frac_of_nominal "
+                               f"uses the nominal {FP64_NOMINAL_GFLOPS:.0f} GFLOP/s")
+    out["how"] = ("forward and adjoint of one model, each timed on its own; fp64_frac counts "
+                  "node evaluations only (the background, reductions and assembly are in the "
+                  "time)")
     return out
 
 
@@ -507,26 +595,40 @@ def run_batched(args, rank, world, local):
     ms_per_step = total_ms / args.steps
     value = units * world * args.steps / (total_ms * 1e-3) / 1e6
 
-    # accuracy of the mixed path against the FP64 matrix-free path (model 0, 1)
+    # accuracy of the mixed path against the FP64 matrix-free path: four
+    # models at all stations (data and gradient of the step's misfit), and
+    # the data of all models at every eighth station
     errs = {"data_gz": 0.0, "data_ftg": 0.0, "grad": 0.0,
             "max_abs_data_gz": 0.0, "max_abs_data_ftg": 0.0, "max_abs_grad": 0.0}
-    for i in (0, nmod - 1):
-        ref = torch.zeros(n * 10, dtype=torch.float64, device=dev)
-        gref = torch.zeros(s.nparm, dtype=torch.float64, device=dev)
+    ref = torch.zeros(n * 10, dtype=torch.float64, device=dev)
+    gref = torch.zeros(s.nparm, dtype=torch.float64, device=dev)
+    rel = lambda x, y: float(torch.linalg.norm(x - y) / torch.linalg.norm(y))
+    for i in (0, nmod // 3, (2 * nmod) // 3, nmod - 1):
         ctx.forward_device(models[i].data_ptr(), ref.data_ptr())
         ctx.lqderivative_device(models[i].data_ptr(), misfit[i].data_ptr(), gref.data_ptr())
         ctx.synchronize()
         a, r = data[i].view(n, 10), ref.view(n, 10)
-        errs["data_gz"] = max(errs["data_gz"], float(torch.linalg.norm(a[:, 0] - r[:, 0]) /
-                                                     torch.linalg.norm(r[:, 0])))
-        errs["data_ftg"] = max(errs["data_ftg"], float(torch.linalg.norm(a[:, 1:] - r[:, 1:]) /
-                                                       torch.linalg.norm(r[:, 1:])))
-        errs["grad"] = max(errs["grad"], float(torch.linalg.norm(grads[i] - gref) /
-                                               torch.linalg.norm(gref)))
-        for key, x, ref_ in (("max_abs_data_gz", a[:, 0], r[:, 0]),
-                             ("max_abs_data_ftg", a[:, 1:], r[:, 1:]),
-                             ("max_abs_grad", grads[i], gref)):
-            errs[key] = max(errs[key], float((x - ref_).abs().max()))
+        for key, x, y in (("data_gz", a[:, 0], r[:, 0]), ("data_ftg", a[:, 1:], r[:, 1:]),
+                          ("grad", grads[i], gref)):
+            errs[key] = max(errs[key], rel(x, y))
+            errs["max_abs_" + key] = max(errs["max_abs_" + key], float((x - y).abs().max()))
+    sub_idx = np.arange(0, n, 8)
+    sctx = capi.Context(local)
+    sctx.set_stream(stream.cuda_stream)
+    W.setup_context(sctx, s.subset(sub_idx))
+    sref = torch.zeros(sub_idx.size * 10, dtype=torch.float64, device=dev)
+    sub_t = torch.tensor(sub_idx, device=dev)
+    sub_worst = {"data_gz": 0.0, "data_ftg": 0.0}
+    for i in range(nmod):
+        sctx.forward_device(models[i].data_ptr(), sref.data_ptr())
+        a, r = data[i].view(n, 10)[sub_t], sref.view(-1, 10)
+        sub_worst["data_gz"] = max(sub_worst["data_gz"], rel(a[:, 0], r[:, 0]))
+        sub_worst["data_ftg"] = max(sub_worst["data_ftg"], rel(a[:, 1:], r[:, 1:]))
+    sctx.close()
+    errs["all_models_on_station_subset"] = sub_worst
+    errs["how"] = ("relative norm errors (max over models) and max absolute errors (SI) "
+                   "against the FP64 matrix-free path: 4 models at all 1024 stations (data and "
+                   "gradient); all models' data at 128 stations (every eighth)")
 
     # plain FP64 matrix-free path, one model, same survey (for the ratio)
     plain_t = []
@@ -621,34 +723,35 @@ def run_batched(args, rank, world, local):
                         "how": "j3g_batched_forward / j3g_batched_lqderivative, one at a time"}}
 
     peaks, src = measured_peaks()
-    flops = 3 * 2.0 * R * nmod * K  # per GEMM launch, either direction
+    flops_alg = 2.0 * R * nmod * K  # per product launch, either direction
     gemm_ms = (gf_ms + ga_ms) / max(1, gf_n + ga_n)
-    achieved = flops / (gemm_ms * 1e-3) / 1e12
+    achieved = flops_alg / (gemm_ms * 1e-3) / 1e12
     j_bytes = 2 * R * info["cols"] * 2  # hi + lo read once per launch
     # fp16 and bf16 MMA (kind::f16) share one dense rate; the measured cuBLAS
     # bf16 figure is the denominator
     roof = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"],
             "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"],
-            "traffic": GEMM_DRAM_BYTES_PER_LAUNCH, "traffic_unit": "DRAM bytes per launch",
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
-                              "full-size config-4 launches (mean of forward and adjoint)",
+            "traffic": GEMM_DRAM_BYTES_PER_LAUNCH,
+            "flops_per_launch": flops_alg,
+            "flops_how": "2 x rows x cells x models per product launch (7 stored rows per "
+                         "station), the algorithmic work of one J M or J^T R",
+            "traffic_unit": "DRAM bytes per launch", "traffic_source": GEMM_TRAFFIC_SOURCE,
             # J hi + lo and the forward's model hi + lo, read once; the
-            # per-split partial sums (235-268 MB) come on top
+            # per-split partial sums come on top
             "algorithmic_bytes_per_launch": j_bytes + 4 * nmod * K,
             "peak_source": f"{src} bf16_tflops (burst; fp16 MMA runs at the bf16 rate)",
             "kernel": "k_gemm_pair<fp16> (CTA pair, 256 x 256 tiles, 3 fp16 products per launch)",
             "ms_per_launch": {"forward": gf_ms / max(1, gf_n), "adjoint": ga_ms / max(1, ga_n)},
             "plans": {"forward": ctx.gemm_plan(0), "adjoint": ctx.gemm_plan(1),
                       "how": "autotuned on the first call of each shape (K splits, N tile)"},
-            "hbm_gbs_of_J_stream": j_bytes / (gemm_ms * 1e-3) / 1e9,
+            "executed_frac": 3 * achieved / peaks["bf16_tflops"],
+            "executed_how": "tensor-pipe work actually issued (hi*hi + hi*lo + lo*hi: 3 x the "
+                            "algorithmic flops) over the same peak",
+            "j_stream_gbs": j_bytes / (gemm_ms * 1e-3) / 1e9,
+            "j_stream_hbm_frac": j_bytes / (gemm_ms * 1e-3) / 1e9 / peaks["hbm_gbs"],
             "hbm_peak_gbs": peaks["hbm_gbs"]}
     ctx.close()
-    refinement = measure_refinement(s, nmod, args.steps, stream, flush, local, peaks)
-    stream_fp32 = measure_stream(args.steps, stream, flush, local, peaks)
-    fp64_configs = measure_fp64_configs(stream, flush, local)
-    ftg = data[0].view(n, 10)[:, 1:].reshape(-1).cpu().numpy()
-    netcdf_io = measure_netcdf(s, ftg) if rank == 0 else None
-    return {
+    out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
@@ -659,19 +762,27 @@ def run_batched(args, rank, world, local):
                    "models": nmod, "rows": R, "kind": "joint g_z + FTG",
                    "l2": "flushed between timed steps (512 MiB write); J (3.8 GB per direction) "
                          "exceeds L2",
-                   "sensitivity_build_ms": build_ms, "sensitivity_bytes": info["bytes"],
                    "parallelism": f"replicas{world}"},
-        "err_vs_fp64": errs,  # relative norm errors and maximum absolute errors (SI units)
-        "plain_fp64": {"value": plain_value, "unit": UNIT, "ms_per_step": plain_ms,
-                       "what": "FP64 matrix-free fwd+adjoint of one model, same survey"},
-        "speedup_vs_plain_fp64": value / plain_value,
-        "ms_per_step_by_phase": phase_ms,
+        "sensitivity_build_ms": build_ms, "sensitivity_bytes": info["bytes"],
+        "gpu_launches": launches, "clocks": clk,
         "step": "one CUDA graph per step (batched forward, weighted misfit, batched "
                 "adjoint: %d library kernels + 2 torch kernels), replayed" % launches_per_step,
-        "e2e": e2e, "gpu_launches": launches, "roofline": roof, "clocks": clk,
-        "refinement": refinement, "stream_fp32": stream_fp32, "fp64_configs": fp64_configs,
-        "netcdf": netcdf_io,
+        "ms_per_step_by_phase": phase_ms,
+        "plain_fp64": {"value": plain_value, "unit": UNIT, "ms_per_step": plain_ms,
+                       "what": "FP64 matrix-free fwd+adjoint of one model, same survey"},
     }
+    if args.sections == "all":
+        cpu = rank == 0
+        out["refinement"] = measure_refinement(s, nmod, args.steps, stream, flush, local, peaks)
+        out["stream_fp32"] = measure_stream(args.steps, stream, flush, local, peaks, cpu)
+        out["fp64_configs"] = measure_fp64_configs(stream, flush, local, cpu)
+        ftg = data[0].view(n, 10)[:, 1:].reshape(-1).cpu().numpy()
+        out["netcdf"] = measure_netcdf(s, ftg) if rank == 0 else None
+    out["e2e"] = e2e
+    out["roofline"] = roof
+    out["speedup_vs_plain_fp64"] = value / plain_value
+    out["err_vs_fp64"] = errs
+    return out
 
 
 def run_plain(args, rank, world, local):
@@ -753,96 +864,214 @@ def run_plain(args, rank, world, local):
 # ---------------------------------------------------------------------------
 # CPU baselines (the oracle: the C restatement of the reference's algorithm)
 
-def cpu_cached_products(budget_s=12.0):
+class CachedProductsSample:
     """The reference's cached-sensitivity path on the host
-    (FullSensitivityGravMagCalculator: d = J m, g = 2 J^T r per model, FP64),
-    sensitivity rows of a station sample built once, models spread over all
-    host threads.  Returns (cell*station*model/s in M, cores, sample text)."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from oracle import oracle as O
-    from helpers import oracle_forward
-    from jif3d_gb300 import workloads as W
-    O.build()
-    s = W.config4()
-    n = s.stations.shape[0]
-    nst = 8
-    sub = s.subset(np.arange(nst) * (n // nst))
-    _, J = oracle_forward(O, sub, want_sens=True)   # 80 x 131072 FP64 rows (not timed)
-    J = np.ascontiguousarray(J)
-    cores = os.cpu_count() or 1
-    rng = np.random.default_rng(7)
-    r = rng.normal(size=J.shape[0])
+    (FullSensitivityGravMagCalculator: d = J m, g = 2 J^T r per model, FP64)
+    on the batched workload: the FP64 sensitivity rows of a station sample
+    (32 of the 1024 stations, 320 rows x 131072 cells = 336 MB, more than a
+    host's last-level cache) are built once, untimed; each sample then runs
+    the products of as many models as fit in `budget_s`, spread over all
+    host threads."""
+    NST = 32
 
-    def one(m):
-        O.sens_matvec(J, m)
-        O.sens_rmatvec2(J, r)
+    def __init__(self):
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from oracle import oracle as O
+        from helpers import oracle_forward
+        from jif3d_gb300 import workloads as W
+        O.build()
+        self.O = O
+        self.s = s = W.config4()
+        n = s.stations.shape[0]
+        sub = s.subset(np.arange(self.NST) * (n // self.NST))
+        _, J = oracle_forward(O, sub, want_sens=True)
+        self.J = np.ascontiguousarray(J)
+        self.r = np.random.default_rng(7).normal(size=self.J.shape[0])
+        self.cores = os.cpu_count() or 1
+        self.per_model_s = None
 
-    t0 = time.perf_counter()
-    one(s.models[0])
-    t1 = time.perf_counter() - t0
-    nm = int(max(cores, min(s.models.shape[0], budget_s * cores / max(t1, 1e-4))))
-    models = [s.models[i % s.models.shape[0]] for i in range(nm)]
-    t0 = time.perf_counter()
-    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
-        list(ex.map(one, models))
-    t = time.perf_counter() - t0
-    return (s.ngrid * nst * nm / t / 1e6, cores,
-            f"cached-J products (J m and 2 J^T r, FP64) of {nm} models on {nst} of {n} "
-            f"stations x all {s.ngrid} cells, models spread over {cores} threads")
+    def one(self, m):
+        self.O.sens_matvec(self.J, m)
+        self.O.sens_rmatvec2(self.J, self.r)
 
-
-def cpu_matrix_free(budget_s=10.0):
-    """The reference's OpenMP matrix-free forward + LQDerivative (one model)
-    on a station sample; all host threads."""
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    from oracle import oracle as O
-    from helpers import oracle_forward, oracle_lqderivative
-    from jif3d_gb300 import workloads as W
-    O.build()
-    s = W.config4(nmodels=1)
-    n = s.stations.shape[0]
-
-    def run(k):
-        sub = s.subset(np.arange(k) * max(1, n // k))
+    def sample(self, budget_s):
+        """Returns (Mcell*station*model/s, seconds, models) of one sample."""
+        s = self.s
+        if self.per_model_s is None:
+            t0 = time.perf_counter()
+            self.one(s.models[0])
+            self.per_model_s = time.perf_counter() - t0
+        nm = int(max(self.cores, min(4 * s.models.shape[0],
+                                     budget_s * self.cores / max(self.per_model_s, 1e-4))))
+        models = [s.models[i % s.models.shape[0]] for i in range(nm)]
         t0 = time.perf_counter()
-        d = oracle_forward(O, sub)
-        oracle_lqderivative(O, sub, np.ones(d.size))
+        with cf.ThreadPoolExecutor(max_workers=self.cores) as ex:
+            list(ex.map(self.one, models))
+        t = time.perf_counter() - t0
+        return s.ngrid * self.NST * nm / t / 1e6, t, nm
+
+    def describe(self, nm):
+        n = self.s.stations.shape[0]
+        return (f"cached-J products (J m and 2 J^T r, FP64) of {nm} models on {self.NST} of "
+                f"{n} stations (J {self.J.nbytes / 1e6:.0f} MB, built once) x all "
+                f"{self.s.ngrid} cells, models spread over {self.cores} threads")
+
+
+class MatrixFreeSample:
+    """The reference's OpenMP matrix-free forward + LQDerivative (one model,
+    FP64) on the batched workload's survey, on a station sample sized to
+    `budget_s`; all host threads."""
+
+    def __init__(self):
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from oracle import oracle as O
+        from helpers import oracle_forward, oracle_lqderivative
+        from jif3d_gb300 import workloads as W
+        O.build()
+        self.O, self.fwd, self.lqd = O, oracle_forward, oracle_lqderivative
+        self.s = W.config4(nmodels=1)
+        self.per_station_s = None
+        self.cores = os.cpu_count() or 1
+
+    def _run(self, k):
+        n = self.s.stations.shape[0]
+        sub = self.s.subset(np.arange(k) * max(1, n // k))
+        t0 = time.perf_counter()
+        d = self.fwd(self.O, sub)
+        self.lqd(self.O, sub, np.ones(d.size))
         return time.perf_counter() - t0
 
-    t1 = run(1)
-    k = int(max(1, min(n, budget_s / max(t1, 1e-3))))
-    t = run(k)
-    return (s.ngrid * k / t / 1e6, os.cpu_count() or 1,
-            f"OpenMP matrix-free fwd+adjoint, {k} of {n} stations x all {s.ngrid} cells")
+    def sample(self, budget_s):
+        if self.per_station_s is None:
+            self.per_station_s = self._run(1)
+        n = self.s.stations.shape[0]
+        k = int(max(1, min(n, budget_s / max(self.per_station_s, 1e-3))))
+        t = self._run(k)
+        return self.s.ngrid * k / t / 1e6, t, k
+
+    def describe(self, k):
+        n = self.s.stations.shape[0]
+        return (f"OpenMP matrix-free fwd+adjoint, {k} of {n} stations x all {self.s.ngrid} "
+                f"cells, {self.cores} threads")
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the oracle (the C restatement of the reference's
+    implementation) on the host cores, on the same workload, metric and unit
+    as our arm.  Each of the `--steps` steps is one bounded sample (about
+    150 s / steps of host work, 2 to 10 s each), after up to three untimed
+    warm-up samples of one second on the same sampler (thread pool, pages of
+    the built rows)."""
     if rank != 0:
         return None
-    fn = cpu_cached_products if args.workload == "batched" else cpu_matrix_free
-    # untimed warm-up samples (thread pool, first touch of the rows), then the
-    # timed ones; each sample is bounded to a few seconds of host work
+    sampler = CachedProductsSample() if args.workload == "batched" else MatrixFreeSample()
+    budget = max(2.0, min(10.0, 150.0 / max(1, args.steps)))
     nwarm = min(args.warmup, 3)
     for _ in range(nwarm):
-        fn(budget_s=2.0)
-    vals, cores, sample = [], 1, ""
-    for _ in range(max(1, min(args.steps, 3))):
-        v, cores, sample = fn()
+        sampler.sample(1.0)
+    vals, secs, size = [], [], 0
+    for _ in range(max(1, args.steps)):
+        v, t, size = sampler.sample(budget)
         vals.append(v)
+        secs.append(t)
     v = statistics.median(vals)
+    full_units = 131072 * 1024 * (256 if args.workload == "batched" else 1) / 1e6
     return {
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": len(vals),
-        "warmup": nwarm, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "warmup": nwarm, "ms_per_step": 1e3 * statistics.median(secs),
+        "ms_per_full_step": 1e3 * full_units / v,
+        "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
         "config": {"workload": "config4_batched_64x64x32_" +
                                ("f16x2_256models" if args.workload == "batched"
                                 else "plain_fp64_joint"),
                    "cells": 131072, "stations": 1024,
                    "models": 256 if args.workload == "batched" else 1},
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": sample},
+        "step": "one bounded sample of the workload on the host cores (ms_per_step is its "
+                "time; ms_per_full_step the whole workload at the sample's rate)",
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": sampler.cores, "kind": "port",
+                         "sample": sampler.describe(size)},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+
+
+def run_case(args):
+    """One small, self-contained case of a kernel family (see the module
+    docstring); it runs a few launches and prints one line."""
+    import torch
+    from jif3d_gb300 import capi, workloads as W
+    ctx = capi.Context(0)
+    dev = "cuda:0"
+
+    def thin(s, k):
+        s.subsets = None
+        step = max(1, s.stations.shape[0] // k)
+        return s.subset(np.arange(0, s.stations.shape[0], step)[:k])
+
+    if args.case == "node":
+        s = thin(W.config4(nmodels=1) if args.config == 4 else W.CONFIGS[args.config](),
+                 args.stations)
+        W.setup_context(ctx, s)
+        d = ctx.forward(s.model)
+        g = ctx.lqderivative(s.model, np.ones(d.size))
+        print("node case ok", s.name, s.stations.shape[0], "stations", float(d[0]), float(g[0]))
+    elif args.case == "gemm":
+        s = thin(W.config4(nmodels=args.models), args.stations)
+        W.setup_context(ctx, s)
+        ctx.build_sensitivity(capi.STORE_F16X2)
+        d = ctx.batched_forward(s.models)
+        g = ctx.batched_lqderivative(s.models, np.ones_like(d))
+        print("gemm case ok", s.stations.shape[0], "stations", args.models, "models",
+              float(d[0, 0]), float(g[0, 0]))
+    elif args.case == "stream":
+        s = thin(W.config2(), args.stations)
+        W.setup_context(ctx, s)
+        ctx.build_sensitivity(capi.STORE_FP32)
+        n = s.stations.shape[0]
+        dm = torch.tensor(s.model, dtype=torch.float64, device=dev)
+        dd = torch.zeros(n * 9, dtype=torch.float64, device=dev)
+        dg = torch.zeros(s.nparm, dtype=torch.float64, device=dev)
+        ctx.stored_forward_device(dm.data_ptr(), dd.data_ptr())
+        ctx.stored_lqderivative_device(dm.data_ptr(), dd.data_ptr(), dg.data_ptr())
+        ctx.synchronize()
+        print("stream case ok", n, "stations", float(dd[0]), float(dg[0]))
+    elif args.case == "refine":
+        s = W.config4(nmodels=args.models)
+        half = [np.sort(np.concatenate([c, c[:-1] + 0.5 * np.diff(c)]))
+                for c in (s.coords(0), s.coords(1), s.coords(2))]
+        fine = [capi.refine_axis(s.coords(a), (s.xsize, s.ysize, s.zsize)[a], half[a])
+                for a in range(3)]
+        corner = [np.concatenate([[o], o + np.cumsum(f)[:-1]]) for o, f in zip(s.origin, fine)]
+        ctx.set_mesh(corner[0], corner[1], corner[2], *fine)
+        ctx.set_refinement(s.xsize, s.ysize, s.zsize)
+        coarse = torch.tensor(s.models, dtype=torch.float64, device=dev)
+        refined = torch.zeros((args.models, ctx.sizes()["nparm"]), dtype=torch.float64,
+                              device=dev)
+        back = torch.zeros_like(coarse)
+        ctx.refine_project_device(args.models, coarse.data_ptr(), refined.data_ptr())
+        ctx.refine_combine_device(args.models, refined.data_ptr(), back.data_ptr())
+        ctx.synchronize()
+        print("refine case ok", [f.size for f in fine], args.models, "models",
+              float(back[0, 0]))
+    elif args.case == "batched":
+        s = W.config4(nmodels=args.models)
+        W.setup_context(ctx, s)
+        n = s.stations.shape[0]
+        ctx.build_sensitivity(capi.STORE_F16X2)
+        models = torch.tensor(s.models, dtype=torch.float64, device=dev)
+        nmod = models.shape[0]
+        data = torch.zeros((nmod, n * 10), dtype=torch.float64, device=dev)
+        obs = torch.zeros(n * 10, dtype=torch.float64, device=dev)
+        misfit = torch.zeros_like(data)
+        grads = torch.zeros_like(models)
+        for _ in range(args.steps):
+            ctx.batched_forward_device(nmod, models.data_ptr(), data.data_ptr())
+            torch.sub(data, obs, out=misfit)
+            ctx.batched_lqderivative_device(nmod, models.data_ptr(), misfit.data_ptr(),
+                                            grads.data_ptr())
+        ctx.synchronize()
+        print("batched case ok", n, "stations", nmod, "models", float(grads[0, 0]))
+    ctx.close()
 
 
 def main():
@@ -852,19 +1081,30 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group(backend="nccl" if args.impl == "ours" else "gloo")
-    if args.impl == "reference":
+    if args.case:
+        run_case(args)
+        res = None
+    elif args.impl == "reference":
         res = run_reference(args, rank, world)
     else:
         run = run_batched if args.workload == "batched" else run_plain
         res = run(args, rank, world, local)
         if rank == 0:
-            fn = cpu_cached_products if args.workload == "batched" else cpu_matrix_free
-            v, cores, sample = fn()
-            res["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                                   "sample": sample}
-            if args.workload == "batched":
-                v2, _, sample2 = cpu_matrix_free()
-                res["cpu_baseline_matrix_free"] = {"value": v2, "unit": UNIT, "sample": sample2}
+            smp = CachedProductsSample() if args.workload == "batched" else MatrixFreeSample()
+            v, _, size = smp.sample(12.0)
+            base = {"cpu_baseline": {"value": v, "unit": UNIT, "cores": smp.cores,
+                                     "kind": "port", "sample": smp.describe(size)}}
+            if args.workload == "batched" and args.sections == "all":
+                mf = MatrixFreeSample()
+                v2, _, k = mf.sample(10.0)
+                base["cpu_baseline_matrix_free"] = {"value": v2, "unit": UNIT,
+                                                    "cores": mf.cores, "sample": mf.describe(k)}
+            # the CPU baselines go before the roofline, the speed-up and the
+            # errors, which stay last in the line
+            tail = {k: res.pop(k) for k in ("e2e", "roofline", "speedup_vs_plain_fp64",
+                                            "err_vs_fp64") if k in res}
+            res.update(base)
+            res.update(tail)
     if rank == 0 and res is not None:
         print(json.dumps(res))
     if world > 1:

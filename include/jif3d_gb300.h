@@ -381,22 +381,24 @@ int j3g_get_gemm_plan(const j3g_context *ctx, int direction, int *nsplit, int *t
  * return J3G_ERR_SCRATCH_LIMIT without touching d_data.  Every call shares
  * the array and leaves its last contents behind (each call writes all it
  * reads, nothing needs to start at zero), so calls that overlap on the GPU
- * race on it and must be serialised by the caller.  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress, with that
- * device current); make that first call before any stream capture. */
+ * race on it and must be serialised by the caller.  Each call made outside
+ * stream capture looks up the array's device address on the current device
+ * (cudaGetSymbolAddress), so a device reset between calls is harmless; a call
+ * on a capturing stream reuses the address of the device's last call outside
+ * capture and returns J3G_ERR_STATE if there was none, so make the first call
+ * on a device (and the first after a device reset) before any stream capture. */
 int j3g_forward_noalloc(int kind, int nx, int ny, int nz, const double *d_xnode,
                         const double *d_ynode, const double *d_znode, int nmeas,
                         const double *d_sx, const double *d_sy, const double *d_sz,
                         double inclination, double declination, double field_strength,
                         const double *d_model, double *d_data, void *stream);
 
-/* Measured FP64 FMA rate of the device in GFLOP/s (2 flops per FMA), from a
- * dependent-chain probe kernel; used for the FP64 roofline. */
+/* Measured FP64 FMA rate of the device in GFLOP/s (2 flops per FMA), from
+ * independent FMA chains in a probe kernel of this library; the denominator of
+ * the FP64 roofline fractions that the benchmark reports (no vendor-published
+ * or externally measured FP64 figure is available for the device).  No
+ * counterpart in the reference. */
 int j3g_probe_fp64(j3g_context *ctx, double *gflops);
-/* Launch the four libm probe kernels (loop only, sqrt, log, atan2; n_iter
- * calls per thread) on `device`, for counting FP64 instructions per call with
- * a profiler.  Measurement only; no counterpart in the reference. */
-int j3g_probe_math(int device, int n_iter);
 
 #ifdef __cplusplus
 }

@@ -96,7 +96,6 @@ SIGNATURES = {
     "j3g_nc_close_writer": (_I, [_VP]),
     "j3g_nc_discard_writer": (_I, [_VP]),
     "j3g_probe_fp64": (_I, [_VP, _P]),
-    "j3g_probe_math": (_I, [_I, _I]),
     "j3g_forward_noalloc": (_I, [_I, _I, _I, _I, _VP, _VP, _VP, _I, _VP, _VP, _VP, _D, _D, _D,
                                  _VP, _VP, _VP]),
 }

@@ -127,6 +127,8 @@ struct j3g_context {
   Slot slots[kSlots];
   cudaStream_t h2d_stream = nullptr, d2h_stream = nullptr;
   long long next_ticket = 0;
+  // failure codes of calls whose slot was reused before they were waited for
+  std::map<long long, int> failed_tickets;
 
   // optional per-category kernel timing (j3g_set_timing): event pairs
   // recorded on the context's stream around the dominant launches
@@ -1443,6 +1445,12 @@ int pipeline_slot(j3g_context *c, j3g_context::Slot *&slot) {
   }
   if (slot->ticket >= 0) {  // the call before in this slot must have finished
     J3G_CUDA(c, cudaEventSynchronize(slot->d2h));
+    // that call was never waited for: keep its failure for j3g_batched_wait
+    if (*slot->flag != 0) {
+      c->failed_tickets[slot->ticket] = *slot->flag;
+      *slot->flag = 0;
+      cudaMemsetAsync(c->gerr.p, 0, sizeof(int), c->stream);
+    }
     slot->ticket = -1;
   }
   return J3G_OK;
@@ -1575,7 +1583,15 @@ int j3g_batched_wait(j3g_context *c, long long ticket) {
   if (!c || ticket < 0 || ticket >= c->next_ticket)
     return fail(c, J3G_ERR_ARG, "no such pipelined call");
   cudaSetDevice(c->device);
-  // a call that is no longer in its slot has completed (its slot was reused)
+  // a call that is no longer in its slot has completed (its slot was reused);
+  // a failure seen when its slot was reused is reported now
+  auto f = c->failed_tickets.find(ticket);
+  if (f != c->failed_tickets.end()) {
+    const int code = f->second;
+    c->failed_tickets.erase(f);
+    return fail(c, J3G_ERR_CUDA,
+                "tensor-core pipeline wait expired (code " + std::to_string(code) + ")");
+  }
   for (auto &sl : c->slots)
     if (sl.ticket == ticket) {
       J3G_CUDA(c, cudaEventSynchronize(sl.d2h));

@@ -14,6 +14,7 @@
 // on it and must be serialised by the caller.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 
@@ -36,12 +37,22 @@ static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 std::mutex g_setup_mutex;
 double *g_scratch_ptr[kMaxDevices] = {};
 
-// Device address of the scratch array on `device` (looked up once per device,
-// with that device current).
-int scratch_for(int device, double **out) {
+// Device address of the scratch array on `device`, with that device current.
+// Outside stream capture the address is looked up on every call: a device
+// reset (cudaDeviceReset) or a new primary context loads the library's module
+// again, possibly at another address, so a remembered address could be stale.
+// While `stream` is being captured, the address remembered from the last call
+// outside capture is used (looking a symbol up may load the module, which a
+// capturing stream must not see); a first call inside capture is refused.
+int scratch_for(int device, cudaStream_t stream, double **out) {
   if (device < 0 || device >= kMaxDevices) return J3G_ERR_ARG;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    return J3G_ERR_CUDA;
+  }
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[device]) {
+  if (cap == cudaStreamCaptureStatusNone) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
@@ -49,6 +60,8 @@ int scratch_for(int device, double **out) {
       return J3G_ERR_CUDA;
     }
     g_scratch_ptr[device] = static_cast<double *>(p);
+  } else if (!g_scratch_ptr[device]) {
+    return J3G_ERR_STATE;
   }
   *out = g_scratch_ptr[device];
   return J3G_OK;
@@ -94,18 +107,20 @@ extern "C" int j3g_forward_noalloc(int kind, int nx, int ny, int nz, const doubl
          (nn + (npb >> 1) - 1) / (npb >> 1) <= max_blocks)
     npb >>= 1;
   while (spb > 1 && blocks(npb, spb) < 152 * 8) spb >>= 1;
+  // station blocks run over grid y: at most 65535 of them
+  spb = std::max(spb, (nmeas + 65534) / 65535);
   const int nblk = (int)((nn + npb - 1) / npb);
 
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess) return J3G_ERR_CUDA;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
   double *scratch = nullptr;
-  int rc = scratch_for(device, &scratch);
+  int rc = scratch_for(device, st, &scratch);
   if (rc != J3G_OK) return rc;
   double *rho_t = scratch;
   double *comps = scratch + rho_len;
   double *partial = comps + comps_len;
 
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   MeshView m;
   m.nx = nx;
   m.ny = ny;

@@ -33,16 +33,17 @@ _lib = None
 _ref = None
 
 
-def build(force: bool = False) -> None:
-    """Compile liboracle.so (and the reference box-term library when the
-    jif3D sources exist on this machine)."""
+def build(force: bool = False, ref_src: str | None = None) -> None:
+    """Compile liboracle.so; with `ref_src` (the jif3D source tree, or the
+    JIF3D_REF environment variable) also the reference box-term library,
+    when that tree exists on this machine."""
     srcs = [os.path.join(HERE, f) for f in ("prism_oracle.c", "refine_oracle.c")]
     stale = not os.path.exists(LIB_PATH) or any(
         os.path.getmtime(f) > os.path.getmtime(LIB_PATH) for f in srcs)
     if force or stale:
         subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    ref_src = os.environ.get("JIF3D_REF", "/root/reference/jif3D")
-    if os.path.isdir(ref_src) and (force or not os.path.exists(REF_PATH)):
+    ref_src = ref_src or os.environ.get("JIF3D_REF")
+    if ref_src and os.path.isdir(ref_src) and (force or not os.path.exists(REF_PATH)):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_src}"], check=True)
 
 
@@ -68,6 +69,8 @@ def lib():
         _lib.orc_forward.restype = _I
         _lib.orc_lqderivative.argtypes = common + [_P, _P, _P]
         _lib.orc_lqderivative.restype = _I
+        _lib.orc_forward_lqderivative.argtypes = common + [_P, _P, _P, _P]
+        _lib.orc_forward_lqderivative.restype = _I
         _lib.orc_sens_matvec.argtypes = [_I, _I, _P, _P, _P]
         _lib.orc_sens_rmatvec2.argtypes = [_I, _I, _P, _P, _P]
         _lib.orc_refine_axis.argtypes = [_I, _P, _P, _I, _P, _P]
@@ -185,6 +188,18 @@ class Problem:
         rc = lib().orc_lqderivative(*self._common(), _ptr(model), _ptr(misfit), _ptr(grad))
         assert rc == 0
         return grad
+
+    def forward_lqderivative(self, model, misfit):
+        """forward(model) and lqderivative(model, misfit) from one station
+        loop (the box terms evaluated once for both)."""
+        model, misfit = _f64(model), _f64(misfit)
+        assert model.size == self.nparm and misfit.size == self.nmeas * self.dpm
+        data = np.zeros(self.nmeas * self.dpm)
+        grad = np.zeros(self.nparm)
+        rc = lib().orc_forward_lqderivative(*self._common(), _ptr(model), _ptr(misfit),
+                                            _ptr(data), _ptr(grad))
+        assert rc == 0
+        return data, grad
 
 
 def sens_matvec(J, m):

@@ -532,13 +532,18 @@ int orc_forward(int nx, int ny, int nz, const double *xc, const double *yc, cons
 }
 
 /* Least-squares derivative 2 * sum_i (T_i' J_i)^T misfit_i, the matrix-free
- * loop of GravMag/ThreeDGravMagImplementation.h:177-231. */
-int orc_lqderivative(int nx, int ny, int nz, const double *xc, const double *yc,
-                     const double *zc, const double *xs, const double *ys, const double *zs,
-                     int nbg, const double *bg_thick, int nmeas, const double *mx,
-                     const double *my, const double *mz, int kind, double inc, double dec,
-                     double fs, int transform, double t_inc, double t_dec, int nthreads,
-                     const double *model, const double *misfit, double *grad)
+ * loop of GravMag/ThreeDGravMagImplementation.h:177-231.  With `data` not
+ * NULL the same station loop also stores the forward response, as
+ * orc_forward computes it (the rows and the gridded + background sums of a
+ * station are the same in both loops), so that a test needs one pass over
+ * the box terms for both outputs. */
+int orc_forward_lqderivative(int nx, int ny, int nz, const double *xc, const double *yc,
+                             const double *zc, const double *xs, const double *ys,
+                             const double *zs, int nbg, const double *bg_thick, int nmeas,
+                             const double *mx, const double *my, const double *mz, int kind,
+                             double inc, double dec, double fs, int transform, double t_inc,
+                             double t_dec, int nthreads, const double *model,
+                             const double *misfit, double *data, double *grad)
 {
   orc_problem p = make_problem(nx, ny, nz, xc, yc, zc, xs, ys, zs, nbg, bg_thick, nmeas, mx,
                                my, mz, kind, inc, dec, fs, transform, t_inc, t_dec, nthreads);
@@ -558,6 +563,13 @@ int orc_lqderivative(int nx, int ny, int nz, const double *xc, const double *yc,
     background(&p, s, xw, yw, zw, model + ngrid, b, rows, ncol, ngrid);
     for (int c = 0; c < raw; ++c)
       cur[c] = g[c] + b[c];
+    if (data) {
+      if (transform != ORC_T_NONE)
+        data[s] = apply_transform(&p, cur);
+      else
+        for (int c = 0; c < raw; ++c)
+          data[(size_t)s * dpm + c] = cur[c];
+    }
     if (transform != ORC_T_NONE) {
       /* NewSensitivities = TransDeriv * CurrentSensitivities (1 x raw times raw x ncol) */
       double d[9];
@@ -582,6 +594,18 @@ int orc_lqderivative(int nx, int ny, int nz, const double *xc, const double *yc,
     grad[c] = 2.0 * grad[c];
   free(rows);
   return 0;
+}
+
+int orc_lqderivative(int nx, int ny, int nz, const double *xc, const double *yc,
+                     const double *zc, const double *xs, const double *ys, const double *zs,
+                     int nbg, const double *bg_thick, int nmeas, const double *mx,
+                     const double *my, const double *mz, int kind, double inc, double dec,
+                     double fs, int transform, double t_inc, double t_dec, int nthreads,
+                     const double *model, const double *misfit, double *grad)
+{
+  return orc_forward_lqderivative(nx, ny, nz, xc, yc, zc, xs, ys, zs, nbg, bg_thick, nmeas, mx,
+                                  my, mz, kind, inc, dec, fs, transform, t_inc, t_dec, nthreads,
+                                  model, misfit, NULL, grad);
 }
 
 /* Cached-sensitivity products of GravMag/FullSensitivityGravMagCalculator.h:

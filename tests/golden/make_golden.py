@@ -14,7 +14,7 @@
   stored output.
 
 Run here, where the reference sources exist:
-    python tests/golden/make_golden.py [path/to/jif3D]
+    python tests/golden/make_golden.py <path/to/jif3D>
 The GPU machine has no reference tree; tests there read the committed JSON.
 """
 import json
@@ -63,7 +63,9 @@ def box_cases(rng):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/jif3D"
+    if len(sys.argv) < 2:
+        raise SystemExit("usage: make_golden.py <jif3D source tree>")
+    ref_root = sys.argv[1]
     os.environ["JIF3D_REF"] = ref_root
     from oracle import oracle as O
     O.build()

@@ -39,6 +39,21 @@ def oracle_lqderivative(O, s, misfit, model=None):
     return g + t
 
 
+def oracle_forward_lqderivative(O, s, misfit, model=None):
+    """oracle_forward and oracle_lqderivative from one pass over the box terms."""
+    model = s.model if model is None else model
+    if s.kind != W.JOINT:
+        return oracle_problem(O, s).forward_lqderivative(model, misfit)
+    n = s.stations.shape[0]
+    m = np.asarray(misfit).reshape(n, 10)
+    dg, gg = oracle_problem(O, s, W.SCALAR, W.T_NONE).forward_lqderivative(model,
+                                                                          m[:, 0].copy())
+    dt, gt = oracle_problem(O, s, W.TENSOR, W.T_NONE).forward_lqderivative(
+        model, m[:, 1:].ravel().copy())
+    d = np.concatenate([dg.reshape(n, 1), dt.reshape(n, 9)], axis=1).ravel()
+    return d, gg + gt
+
+
 def relerr(x, ref):
     x, ref = np.asarray(x, float), np.asarray(ref, float)
     den = np.linalg.norm(ref)

@@ -12,8 +12,8 @@ import math
 import numpy as np
 import pytest
 
-from helpers import (maxrel, oracle_forward, oracle_lqderivative, oracle_problem, relerr,
-                     small_survey)
+from helpers import (maxrel, oracle_forward, oracle_forward_lqderivative, oracle_lqderivative,
+                     oracle_problem, relerr, small_survey)
 from jif3d_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -173,10 +173,18 @@ def test_config1_full(ctx, oracle_lib):
 
 
 def test_config2_subset_and_adjoint_identity(ctx, oracle_lib):
+    """Config 2 (FTG, 64 x 64 x 32 cells): 134 of its 1600 stations (every
+    twelfth) against the oracle, data and gradient; at full size the adjoint
+    identity."""
     s = W.config2()
-    sub = s.subset(np.arange(0, 1600, 97))
-    d = gpu(ctx, sub).forward(sub.model)
-    assert relerr(d, oracle_forward(oracle_lib, sub)) <= TOL
+    sub = s.subset(np.arange(0, 1600, 12))
+    misfit = np.random.default_rng(21).normal(size=sub.stations.shape[0] * 9)
+    c = gpu(ctx, sub)
+    d = c.forward(sub.model)
+    g = c.lqderivative(sub.model, misfit)
+    dref, gref = oracle_forward_lqderivative(oracle_lib, sub, misfit)
+    assert relerr(d, dref) <= TOL, relerr(d, dref)
+    assert relerr(g, gref) <= TOL, relerr(g, gref)
     # full size: <J m, r> = <m, J^T r> (LQDerivative returns 2 J^T r)
     c = gpu(ctx, s)
     rng = np.random.default_rng(9)
@@ -194,17 +202,20 @@ def test_config3_gradient_subset_and_fd(ctx, oracle_lib):
     """Joint g_z + FTG weighted gradient: oracle LQDerivative on a station
     subset, and central differences (relative step 1e-4) on seeded cells."""
     s = W.config3()
-    sub = s.subset(np.arange(0, 2500, 313))
+    sub = s.subset(np.arange(0, 2500, 19))  # 132 stations
     rng = np.random.default_rng(31)
     n = sub.stations.shape[0]
     sigma = np.tile(np.array([1e-8] + [1e-9] * 9), n)
     r = sigma * rng.normal(size=n * 10)
     misfit = r / sigma ** 2
-    g = gpu(ctx, sub).lqderivative(sub.model, misfit)
-    ref = oracle_lqderivative(oracle_lib, sub, misfit)
+    c = gpu(ctx, sub)
+    d = c.forward(sub.model)
+    g = c.lqderivative(sub.model, misfit)
+    dref, ref = oracle_forward_lqderivative(oracle_lib, sub, misfit)
+    dg, dt = d.reshape(n, 10), dref.reshape(n, 10)
+    assert relerr(dg[:, 0], dt[:, 0]) <= TOL and relerr(dg[:, 1:], dt[:, 1:]) <= TOL
     assert relerr(g, ref) <= TOL, relerr(g, ref)
     # central differences of phi(m) = sum (d(m) - d_obs)^2 / sigma^2 around d_obs = d(m0) - r
-    c = gpu(ctx, sub)
     d0 = c.forward(sub.model)
     obs = d0 - r
     phi = lambda m: float(np.sum((c.forward(m) - obs) ** 2 / sigma ** 2))

@@ -326,6 +326,54 @@ def test_config4_batched_full(ctx, oracle_lib):
     check_groups(sub, dsub, oracle_forward(oracle_lib, sub, s.models[5]))
 
 
+def test_config4_all_models_on_station_subset(oracle_lib):
+    """Config 4 at full size, every one of the 256 models checked: the
+    batched data of 128 stations (every eighth) against the FP64 matrix-free
+    forward of those stations, and the batched gradients of misfits that are
+    non-zero on those stations only against the FP64 matrix-free gradient of
+    the same misfits; g_z, tensor and gradient groups each <= 1e-6."""
+    import torch
+    s = W.config4()
+    n = s.stations.shape[0]
+    idx = np.arange(0, n, 8)
+    sub = s.subset(idx)
+    big, small = capi.Context(0), capi.Context(0)
+    try:
+        W.setup_context(big, s)
+        big.build_sensitivity(capi.STORE_F16X2)
+        models = dev(s.models)
+        data = torch.zeros((256, n * 10), dtype=torch.float64, device="cuda")
+        big.batched_forward_device(256, models.data_ptr(), data.data_ptr())
+        rng = np.random.default_rng(41)
+        mis_sub = rng.normal(size=(256, idx.size, 10)) * np.array([1e8] + [1e9] * 9)
+        mis_h = np.zeros((256, n, 10))
+        mis_h[:, idx, :] = mis_sub
+        mis = dev(mis_h.reshape(256, n * 10))
+        grads = torch.zeros_like(models)
+        big.batched_lqderivative_device(256, models.data_ptr(), mis.data_ptr(), grads.data_ptr())
+        big.synchronize()
+        data_h = data.cpu().numpy().reshape(256, n, 10)[:, idx, :].reshape(256, -1)
+        grads_h = grads.cpu().numpy()
+        W.setup_context(small, sub)
+        ref = torch.zeros(idx.size * 10, dtype=torch.float64, device="cuda")
+        gref = torch.zeros(s.nparm, dtype=torch.float64, device="cuda")
+        ms = dev(mis_sub.reshape(256, -1))
+        worst = [0.0, 0.0, 0.0]
+        for i in range(256):
+            small.forward_device(models[i].data_ptr(), ref.data_ptr())
+            small.lqderivative_device(models[i].data_ptr(), ms[i].data_ptr(), gref.data_ptr())
+            small.synchronize()
+            r = ref.cpu().numpy().reshape(-1, 10)
+            got = data_h[i].reshape(-1, 10)
+            e = [relerr(got[:, 0], r[:, 0]), relerr(got[:, 1:], r[:, 1:]),
+                 relerr(grads_h[i], gref.cpu().numpy())]
+            worst = [max(a, b) for a, b in zip(worst, e)]
+        assert max(worst) <= TOL, worst
+    finally:
+        big.close()
+        small.close()
+
+
 def test_batched_step_captured_in_cuda_graph(ctx, oracle_lib):
     """One batched step (forward, weighted misfit, adjoint) captured in a CUDA
     graph after a warm-up call and replayed on new models written in place:

@@ -189,6 +189,20 @@ def test_lqderivative_equals_2JTr(oracle_lib, kind):
     np.testing.assert_allclose(g, ref, rtol=1e-12, atol=1e-12 * np.abs(ref).max())
 
 
+@pytest.mark.parametrize("kind,transform", [(W.SCALAR, W.T_NONE), (W.TENSOR, W.T_FTG_INVARIANT),
+                                            (W.MAGNETIC, W.T_TFA), (W.MAGNETIC, W.T_NONE)])
+def test_fused_forward_lqderivative_is_both_calls(oracle_lib, kind, transform):
+    """The one-pass oracle call gives the forward and the derivative of the
+    two separate calls bit for bit."""
+    O = oracle_lib
+    s = small_survey(kind, seed=17 + kind, transform=transform)
+    p = oracle_problem(O, s)
+    r = np.random.default_rng(2).normal(size=s.stations.shape[0] * s.dpm)
+    d, g = p.forward_lqderivative(s.model, r)
+    assert np.array_equal(d, p.forward(s.model))
+    assert np.array_equal(g, p.lqderivative(s.model, r))
+
+
 def test_ftg_invariant_kat():
     """Gravity/test_transforms.cpp:27-56."""
     from jif3d_gb300.gravmag import FTGInvariant

@@ -62,6 +62,36 @@ def test_noalloc_matches_allocating_forward_twice(kind):
     ctx.close()
 
 
+@pytest.mark.parametrize("kind", [W.SCALAR, W.JOINT])
+def test_noalloc_larger_call_then_smaller_call(kind):
+    """A large problem fills more of the shared scratch (more node blocks of
+    partial sums, component sums at other offsets); the smaller problem after
+    it must not read anything the large one left behind."""
+    import torch
+    lib = capi.load()
+    dev = torch.device("cuda", 0)
+    f64 = dict(dtype=torch.float64, device=dev)
+    for n, (nx, ny, nz, nmeas) in enumerate(((40, 31, 12, 211), (9, 7, 5, 11))):
+        s = small_survey(kind, nx=nx, ny=ny, nz=nz, nmeas=nmeas, seed=700 + 10 * kind + n,
+                         bg=False)
+        d_nodes = [torch.tensor(s.coords(a), **f64) for a in range(3)]
+        d_st = [torch.tensor(np.ascontiguousarray(s.stations[:, a]), **f64) for a in range(3)]
+        ctx = capi.Context(0)
+        W.setup_context(ctx, s)
+        d_model = torch.tensor(s.model, **f64)
+        d_ref = torch.zeros(nmeas * s.raw, **f64)
+        d_out = torch.full_like(d_ref, float("nan"))
+        ctx.forward_device(d_model.data_ptr(), d_ref.data_ptr())
+        ctx.synchronize()
+        rc = _noalloc(lib, s, d_nodes, d_st, d_model, d_out)
+        assert rc == capi.OK, lib.j3g_status_string(rc)
+        torch.cuda.synchronize()
+        out, ref = d_out.cpu().numpy(), d_ref.cpu().numpy()
+        assert np.all(np.isfinite(out))
+        assert relerr(out, ref) <= TOL, ((nx, ny, nz, nmeas), relerr(out, ref))
+        ctx.close()
+
+
 def test_noalloc_rejects_problems_beyond_its_scratch():
     import torch
     lib = capi.load()
