@@ -339,7 +339,9 @@ int j3g_get_timing(j3g_context *ctx, int category, double *total_ms, long long *
 
 /* Autotuning of the tensor-core products (J3G_STORE_F16X2 batched calls); no
  * reference counterpart.  Off by default: a fixed rule picks the K-split count
- * and the N tile.  With enable = 1, the first product of each shape (direction,
+ * and the N tile (about six waves of CTAs, at most 64 k-blocks per split), so
+ * a caller that never calls this -- the unchanged jif3D calculators through
+ * the C++ implementation, for one -- runs untuned plans.  With enable = 1, the first product of each shape (direction,
  * rows, models, K) times a few candidate plans -- split counts that fill the
  * last wave of CTAs, and one-SM 128-wide tiles in place of CTA pairs -- and
  * keeps the fastest for the context's lifetime.  Every candidate keeps the
@@ -359,6 +361,19 @@ int j3g_set_gemm_plan(j3g_context *ctx, int direction, int nsplit, int tile);
  * the autotuner's time of that plan in ms (0 for the fixed rule). */
 int j3g_get_gemm_plan(const j3g_context *ctx, int direction, int *nsplit, int *tile,
                       double *tuned_ms);
+/* Failure-path test of the tensor-core products' bounded waits; no
+ * counterpart in the reference (whose CUDA layer exits on any error,
+ * Global/CudaError.h:13-22).  With fault = 1, every later tensor-core product
+ * launch of this context simulates a stalled pipeline without faulting the
+ * GPU: its drain warps withhold the releases of their TMEM accumulators, the
+ * MMA issuer gives up on one after 20 ms, stops issuing and waits for the
+ * MMAs and copies it has issued (each wait bounded by 2 s), and the launch
+ * records an error code; the call that checks the flag (j3g_synchronize,
+ * j3g_batched_forward / _lqderivative, j3g_batched_wait) returns
+ * J3G_ERR_CUDA and clears it, and the context stays usable.  A launch
+ * takes about 2 s in this mode and its results are not defined.  fault = 0
+ * restores the normal path.  Test use only. */
+int j3g_set_test_fault(j3g_context *ctx, int fault);
 
 /* Allocation-free gridded forward, for callers that cannot let a library
  * allocate device memory: hosts that reserve all device memory for their own

@@ -96,6 +96,7 @@ SIGNATURES = {
     "j3g_nc_close_writer": (_I, [_VP]),
     "j3g_nc_discard_writer": (_I, [_VP]),
     "j3g_probe_fp64": (_I, [_VP, _P]),
+    "j3g_set_test_fault": (_I, [_VP, _I]),
     "j3g_forward_noalloc": (_I, [_I, _I, _I, _I, _VP, _VP, _VP, _I, _VP, _VP, _VP, _D, _D, _D,
                                  _VP, _VP, _VP]),
 }
@@ -575,6 +576,10 @@ class Context:
         self._check(self._lib.j3g_get_timing(self._h, int(category), ctypes.byref(ms),
                                              ctypes.byref(n)))
         return ms.value, n.value
+
+    def set_test_fault(self, fault):
+        """Failure-path test of the tensor-core waits (see j3g_set_test_fault)."""
+        self._check(self._lib.j3g_set_test_fault(self._h, int(fault)))
 
     def launch_count(self):
         v = _LL()

@@ -129,6 +129,8 @@ struct j3g_context {
   long long next_ticket = 0;
   // failure codes of calls whose slot was reused before they were waited for
   std::map<long long, int> failed_tickets;
+  // j3g_set_test_fault: the fault the tensor-core launches simulate (0: none)
+  int test_fault = 0;
 
   // optional per-category kernel timing (j3g_set_timing): event pairs
   // recorded on the context's stream around the dominant launches
@@ -794,17 +796,19 @@ int gemm_plan(j3g_context *c, int dir, const GemmOperands &g, long long ldp, lon
 
   J3G_TRY(ensure(c, c->P, sizeof(float) * (size_t)nsp_max * slice));
   float *P = ptr<float>(c->P);
+  GemmOperands gt = g;
+  gt.fault = 0;  // candidates are timed on the normal path
   cudaEvent_t a, b;
   J3G_CUDA(c, cudaEventCreate(&a));
   J3G_CUDA(c, cudaEventCreate(&b));
   float best = 0.0f;
   for (auto &p : cand) {
     float ms = 0.0f;
-    cudaError_t e = launch_gemm_x3(g, p.second, P, ldp, slice, ptr<int>(c->gerr), c->stream,
+    cudaError_t e = launch_gemm_x3(gt, p.second, P, ldp, slice, ptr<int>(c->gerr), c->stream,
                                    p.first);
     if (e == cudaSuccess) e = cudaEventRecord(a, c->stream);
     if (e == cudaSuccess)
-      e = launch_gemm_x3(g, p.second, P, ldp, slice, ptr<int>(c->gerr), c->stream, p.first);
+      e = launch_gemm_x3(gt, p.second, P, ldp, slice, ptr<int>(c->gerr), c->stream, p.first);
     if (e == cudaSuccess) e = cudaEventRecord(b, c->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(b);
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
@@ -867,6 +871,7 @@ int batched_forward_pass(j3g_context *c, int nmod, const double *d_models, doubl
     }
     const long long slice = (long long)nmod * R;
     GemmOperands g{c->Jhi.p, c->Jlo.p, R, c->Bhi.p, c->Blo.p, nmod, npad, ldK, true};
+    g.fault = c->test_fault;
     J3G_TRY(ensure(c, c->gerr, sizeof(int)));
     j3g_context::GemmPlan plan;
     J3G_TRY(gemm_plan(c, 0, g, R, slice, plan));
@@ -949,6 +954,7 @@ int batched_adjoint_pass(j3g_context *c, int nmod, const double *d_models,
     }
     const long long slice = (long long)nmod * K;
     GemmOperands g{c->JThi.p, c->JTlo.p, K, c->Bhi.p, c->Blo.p, nmod, npad, ldR, true};
+    g.fault = c->test_fault;
     J3G_TRY(ensure(c, c->gerr, sizeof(int)));
     j3g_context::GemmPlan plan;
     J3G_TRY(gemm_plan(c, 1, g, K, slice, plan));
@@ -1673,6 +1679,13 @@ int j3g_set_autotune(j3g_context *c, int enable) {
   if (!c) return J3G_ERR_ARG;
   c->autotune = enable != 0;
   ++c->prod_gen;
+  return J3G_OK;
+}
+
+int j3g_set_test_fault(j3g_context *c, int fault) {
+  if (!c || fault < 0 || fault > 1) return J3G_ERR_ARG;
+  c->test_fault = fault;
+  ++c->prod_gen;  // captured products hold the old kernel arguments
   return J3G_OK;
 }
 

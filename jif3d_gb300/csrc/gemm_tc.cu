@@ -49,6 +49,12 @@ constexpr int kStepsPerDrain = 2;
 constexpr int kDrainsPerBlock = (BK / 16) / kStepsPerDrain;
 constexpr int kAccBufs = 4;  // TMEM accumulators in rotation (4 x BN columns)
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
+// With the test fault (GemmOperands::fault) the drain warps withhold their
+// accumulator releases and the MMA issuer gives up on a release after this
+// long; every other wait keeps kWaitNs, so that no copy or MMA is still in
+// flight when the CTA tears down.  The failure path of the bounded waits is
+// tested this way, with no GPU fault.
+constexpr unsigned long long kTestWaitNs = 20000000ull;  // 20 ms
 
 template <int BN, bool F16> struct Cfg {
   static constexpr int STAGES = BN == 128 ? 3 : 4;
@@ -100,13 +106,14 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait: true when the phase completed, false after the deadline.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// Bounded wait: true when the phase completed, false after `limit_ns`.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity,
+                                          unsigned long long limit_ns = kWaitNs) {
   if (mbar_try(bar, parity)) return true;
   const unsigned long long t0 = now_ns();
   while (true) {
     if (mbar_try(bar, parity)) return true;
-    if (now_ns() - t0 > kWaitNs) return false;
+    if (now_ns() - t0 > limit_ns) return false;
   }
 }
 
@@ -209,7 +216,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     k_gemm_x3(const __grid_constant__ CUtensorMap tmAhi, const __grid_constant__ CUtensorMap tmAlo,
               const __grid_constant__ CUtensorMap tmBhi, const __grid_constant__ CUtensorMap tmBlo,
               int kb_per_split, int kb_total, int M, int N, int ntn, float *__restrict__ P,
-              long long ldp, long long slice, int *__restrict__ err) {
+              long long ldp, long long slice, int *__restrict__ err, int fault) {
   using C = Cfg<BN, F16>;
   constexpr int S = C::STAGES;
   extern __shared__ uint8_t smem_raw[];
@@ -304,7 +311,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
           const int d = i * kDrainsPerBlock + j;
           const int b = d % kAccBufs;
           if (d >= kAccBufs &&
-              !mbar_wait(smem_u32(a_empty + b), ((uint32_t)(d / kAccBufs) & 1u) ^ 1u)) {
+              !mbar_wait(smem_u32(a_empty + b), ((uint32_t)(d / kAccBufs) & 1u) ^ 1u,
+                         fault ? kTestWaitNs : kWaitNs)) {
             // the buffer of drain d - kAccBufs was never emptied
             atomicExch(err, 3);
             ok = false;
@@ -363,7 +371,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       }
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(smem_u32(a_empty + b));
+      if (lane == 0 && !fault) mbar_arrive(smem_u32(a_empty + b));
     }
     const int row = m0 + q * 32 + lane;
     float *out = P + (long long)blockIdx.z * slice;
@@ -509,7 +517,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
                 const __grid_constant__ CUtensorMap tmBhi,
                 const __grid_constant__ CUtensorMap tmBlo, int kb_per_split, int kb_total, int M,
                 int N, float *__restrict__ P, long long ldp, long long slice,
-                int *__restrict__ err) {
+                int *__restrict__ err, int fault) {
   using C = PairCfg<F16>;
   constexpr int S = C::STAGES;
   extern __shared__ uint8_t smem_raw[];
@@ -564,12 +572,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
       for (int i = 0; i < nkb; ++i) {
         const int s = i % S;
         const uint32_t ph = (uint32_t)(i / S) & 1u;
+        // no early exit on this CTA's fail flag: both producers stop at the
+        // same k-block (the empty commits reach both CTAs), so the even CTA's
+        // wait below covers every copy the odd CTA issued
         if (i >= S && !mbar_wait(smem_u32(empty + s), ph ^ 1u)) {
           atomicExch(err, 1);
           *fail = 1;
           break;
         }
-        if (*fail) break;
         uint8_t *st = smem + s * C::STAGE_BYTES;
         const uint32_t fb_local = smem_u32(full + s);
         if (rank == 0) mbar_expect_tx(fb_local, 2u * (uint32_t)C::STAGE_BYTES);
@@ -609,7 +619,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
           const int d = i * kDrainsPerBlock + j;
           const int b = d % kPairAcc;
           if (d >= kPairAcc &&
-              !mbar_wait(smem_u32(a_empty + b), ((uint32_t)(d / kPairAcc) & 1u) ^ 1u)) {
+              !mbar_wait(smem_u32(a_empty + b), ((uint32_t)(d / kPairAcc) & 1u) ^ 1u,
+                         fault ? kTestWaitNs : kWaitNs)) {
             atomicExch(err, 3);
             ok = false;
             break;
@@ -678,7 +689,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
       __syncwarp();
       // accumulator b is reused by drain d + kPairAcc: one relaxed arrival per
       // drain warp once its loads are complete (no named barrier per drain)
-      if (lane == 0 && d + kPairAcc < ndrain) {
+      if (lane == 0 && d + kPairAcc < ndrain && !fault) {
         if (rank == 0)
           mbar_arrive(smem_u32(a_empty + b));
         else
@@ -790,7 +801,7 @@ cudaError_t launch_bn(const GemmOperands &g, int nsplit, float *P, long long ldp
   const long long nmt = (g.m + BM - 1) / BM;
   dim3 grid((unsigned)(nmt * ntn), 1u, (unsigned)nsp);
   k_gemm_x3<BN, F16><<<grid, kGemmThreads, Cfg<BN, F16>::SMEM, st>>>(
-      ah, al, bh, bl, kb_per, kb_total, (int)g.m, (int)g.n, ntn, P, ldp, slice, err);
+      ah, al, bh, bl, kb_per, kb_total, (int)g.m, (int)g.n, ntn, P, ldp, slice, err, g.fault);
   return cudaGetLastError();
 }
 
@@ -811,7 +822,7 @@ cudaError_t launch_pair(const GemmOperands &g, int nsplit, float *P, long long l
   // x: CTA pairs over M (two CTAs of 128 rows each), y: N tiles of 256, z: K splits
   dim3 grid((unsigned)(2 * ((g.m + 255) / 256)), (unsigned)(g.n_pad / kPairN), (unsigned)nsp);
   k_gemm_pair<F16><<<grid, kPairThreads, PairCfg<F16>::SMEM, st>>>(
-      ah, al, bh, bl, kb_per, kb_total, (int)g.m, (int)g.n, P, ldp, slice, err);
+      ah, al, bh, bl, kb_per, kb_total, (int)g.m, (int)g.n, P, ldp, slice, err, g.fault);
   return cudaGetLastError();
 }
 

@@ -85,6 +85,10 @@ struct GemmOperands {
   long long n, n_pad;
   long long ld;
   bool f16;
+  // 1: test the failure path of the bounded waits -- the drain warps
+  // withhold their accumulator releases, so the MMA issuer's wait for one
+  // expires (after 20 ms) and the launch reports an error code (j3g_set_test_fault)
+  int fault = 0;
 };
 int gemm_n_tile(int n);
 int gemm_splits_used(long long ld, int nsplit);
