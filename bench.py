@@ -29,6 +29,10 @@ implementation) on a bounded sample.
   stream  -- FP32 stored-J products, `--stations` of the FTG survey
   refine  -- projection / combination to a 2x2x2 refinement, `--models` models
   batched -- `--steps` batched steps (256 models, all stations), no timing
+  reference-gpu -- the reference's own CUDA layer (Gravity/gravcuda.cu, built
+      from the staged sources) on `--stations` stations of `--config` (1: g_z,
+      2: FTG); prints one JSON line (run as a child process: the reference
+      exits the process on a CUDA error)
 """
 from __future__ import annotations
 
@@ -76,7 +80,8 @@ def parse():
     p.add_argument("--sections", choices=["all", "headline"], default="all",
                    help="headline: only the batched step and its e2e / roofline (no other "
                         "workloads, no CPU baselines)")
-    p.add_argument("--case", choices=["node", "gemm", "stream", "refine", "batched"])
+    p.add_argument("--case", choices=["node", "gemm", "stream", "refine", "batched",
+                                      "reference-gpu"])
     p.add_argument("--stations", type=int, default=64)
     p.add_argument("--config", type=int, default=4, choices=[1, 2, 3, 4, 5])
     return p.parse_args()
@@ -776,6 +781,10 @@ def run_batched(args, rank, world, local):
         out["refinement"] = measure_refinement(s, nmod, args.steps, stream, flush, local, peaks)
         out["stream_fp32"] = measure_stream(args.steps, stream, flush, local, peaks, cpu)
         out["fp64_configs"] = measure_fp64_configs(stream, flush, local, cpu)
+        if rank == 0:
+            out["reference_gpu"] = measure_reference_gpu(
+                local, {1: lambda idx: our_gridded(local, 1, idx),
+                        2: lambda idx: our_gridded(local, 2, idx)})
         ftg = data[0].view(n, 10)[:, 1:].reshape(-1).cpu().numpy()
         out["netcdf"] = measure_netcdf(s, ftg) if rank == 0 else None
     out["e2e"] = e2e
@@ -995,9 +1004,87 @@ def run_reference(args, rank, world):
     }
 
 
+def reference_gpu_case(args):
+    """The reference GPU forward (per-station kernels, row copies to the
+    host, host inner products) on the first `--stations` stations of a
+    workload, after one untimed station; prints a JSON line."""
+    from oracle import refgpu
+    from jif3d_gb300 import workloads as W
+    if refgpu.build() is None:
+        print(json.dumps({"unavailable": "reference CUDA sources not staged in baseline/_ref "
+                                         "(staged by __graft_entry__.build() where the jif3D "
+                                         "tree exists)"}))
+        return
+    s = W.CONFIGS[args.config]()
+    tensor = args.config == 2
+    n = min(args.stations, s.stations.shape[0])
+    step = s.stations.shape[0] // n
+    idx = np.arange(0, step * n, step)
+    corner = [s.coords(a)[:-1] for a in range(3)]
+    refgpu.run(*corner, s.xsize, s.ysize, s.zsize, s.stations[idx[:1]], s.model, tensor)
+    data, _, t_loop, t_prep = refgpu.run(*corner, s.xsize, s.ysize, s.zsize, s.stations[idx],
+                                         s.model, tensor)
+    pairs = s.ngrid * n / 1e6
+    print(json.dumps({"workload": s.name, "stations": n, "station_index": idx.tolist(),
+                      "cells": s.ngrid, "forward_s": t_loop, "prepare_free_s": t_prep,
+                      "forward": pairs / t_loop, "unit": UNIT,
+                      "data": data.ravel().tolist()}))
+
+
+def our_gridded(local, cfg, idx):
+    """Our FP64 matrix-free gridded response (background values zero) at the
+    stations `idx` of a workload, in the reference GPU layer's order: g_z, or
+    Uxx Uxy Uxz Uyy Uyz Uzz."""
+    from jif3d_gb300 import capi, workloads as W
+    s = W.CONFIGS[cfg]()
+    sub = s.subset(idx)
+    ctx = capi.Context(local)
+    W.setup_context(ctx, sub)
+    m = s.model.copy()
+    m[s.ngrid:] = 0.0
+    d = ctx.forward(m)
+    ctx.close()
+    return d if cfg == 1 else d.reshape(-1, 9)[:, [0, 1, 2, 4, 5, 8]].ravel()
+
+
+def measure_reference_gpu(local, ours):
+    """The reference's own CUDA layer beside ours: its forward on the g_z
+    workload (all 400 stations) and on the FTG workload (64 of 1600
+    stations), each in a child process; throughput in Mcell*station/s and
+    its data against our FP64 matrix-free data at the same stations."""
+    out = {}
+    for cfg, nst in ((1, 400), (2, 64)):
+        env = dict(os.environ, CUDA_VISIBLE_DEVICES=os.environ.get("CUDA_VISIBLE_DEVICES",
+                                                                   str(local)))
+        r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--case",
+                            "reference-gpu", "--config", str(cfg), "--stations", str(nst)],
+                           capture_output=True, text=True, env=env, timeout=600)
+        line = r.stdout.strip().splitlines()[-1] if r.stdout.strip() else ""
+        try:
+            res = json.loads(line)
+        except ValueError:
+            res = {"unavailable": f"reference GPU run failed (rc {r.returncode}): "
+                                  f"{r.stderr.strip()[-300:]}"}
+        if "data" in res and cfg in ours:
+            got = np.array(res.pop("data"))
+            ref = ours[cfg](np.array(res.pop("station_index")))
+            res["rel_err_vs_ours"] = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        res.pop("data", None)
+        res.pop("station_index", None)
+        out[f"config{cfg}"] = res
+    out["how"] = ("jif3D Gravity/gravcuda.cu built unmodified for sm_103a (block size 128): one "
+                  "kernel per station (six for FTG), each row copied to page-locked host memory "
+                  "and multiplied by the densities on the host, as Scalar/TensorCudaGravityImp "
+                  "do; forward only (the reference GPU path has no adjoint)")
+    return out
+
+
 def run_case(args):
     """One small, self-contained case of a kernel family (see the module
     docstring); it runs a few launches and prints one line."""
+    if args.case == "reference-gpu":
+        reference_gpu_case(args)
+        return
     import torch
     from jif3d_gb300 import capi, workloads as W
     ctx = capi.Context(0)

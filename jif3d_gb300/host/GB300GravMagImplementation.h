@@ -14,10 +14,24 @@
 // (tests, this repository) define JIF3D_GB300_STANDALONE to use the stand-in
 // declarations of jif3d_compat.h.
 //
-// Transforms: jif3D's base class keeps its VectorTransform private, so the
-// device transform is named here as well (SetGB300Transform, the same choice
-// as the calculator's SetDataTransform); Calculate checks that both give the
-// same number of data per station.
+// Transforms: jif3D's base class keeps its VectorTransform private and its
+// SetDataTransform is not virtual, so an implementation cannot see which
+// transform a calculator set -- only GetDataPerMeasurement.  Two routes:
+//  * unchanged callers that set the transform through the calculator only
+//    (Joint/SetupMagnetics.cpp:206, 254 and the like): the device computes
+//    the raw data (and rows) of all stations in one call; Calculate then runs
+//    the base class's station loop over them, so the base applies its own
+//    transform and calls HandleSensitivities; LQDerivative back-projects each
+//    station's misfit through the base class's own derivative loop (run on a
+//    one-station survey and a model of `raw` parameters whose rows are the
+//    identity, which yields 2 T_i'^T m_i), and the device forms 2 J^T of the
+//    back-projected raw misfit.  A transform that keeps the number of data
+//    per station (jif3D's only one for these data is CopyTransform, the
+//    identity) is not visible and is not needed;
+//  * SetGB300Transform names the transform to the device as well, which then
+//    applies it in the fused epilogues (no per-station host work); Calculate
+//    checks that both give the same number of data per station.  The
+//    device-resident calculator needs this route.
 #pragma once
 
 #include <cstring>
@@ -110,6 +124,7 @@ class GB300GravMagImplementation : public ThreeDGravMagImplementation<DataType> 
   virtual rvec Calculate(const ModelType &Model, const DataType &Data,
                          ThreeDGravMagCalculator<DataType> &Calculator) override {
     Upload(ctx_, Model, Data, Data.GetMeasPosX().size(), 0);
+    if (CalculatorTransformOnly()) return ServedCalculate(Model, Data, Calculator);
     CheckTransform();
     const size_t nmeas = Data.GetMeasPosX().size();
     const size_t raw = RawDataPerMeasurement();
@@ -136,12 +151,14 @@ class GB300GravMagImplementation : public ThreeDGravMagImplementation<DataType> 
   virtual rvec LQDerivative(const ModelType &Model, const DataType &Data,
                             const rvec &Misfit) override {
     Upload(ctx_, Model, Data, Data.GetMeasPosX().size(), 0);
-    CheckTransform();
+    const bool served = CalculatorTransformOnly();
+    if (!served) CheckTransform();
     const size_t nmeas = Data.GetMeasPosX().size();
     if (Misfit.size() != nmeas * this->GetDataPerMeasurement())
       throw FatalException("Misfit does not have the size of the data", __FILE__, __LINE__);
     const std::vector<double> params = gb300_detail::to_vector(Model.GetModelParameters());
-    const std::vector<double> misfit = gb300_detail::to_vector(Misfit);
+    const std::vector<double> misfit =
+        served ? BackProjectedMisfit(params, Data, Misfit) : gb300_detail::to_vector(Misfit);
     std::vector<double> grad(Model.GetNModelParm());
     Check(ctx_, j3g_lqderivative(ctx_, params.data(), misfit.data(), grad.data()),
           "j3g_lqderivative");
@@ -189,17 +206,117 @@ class GB300GravMagImplementation : public ThreeDGravMagImplementation<DataType> 
   }
 
  private:
-  // Per-station parts of the base class's station loop, through a context
-  // holding the one station: the gridded response and rows (columns of the
-  // cell blocks), and the background response and rows (columns ngrid..).
+  // What CalcGridded / CalcBackground return while the base class's loops
+  // run over data computed beforehand (see ServedCalculate,
+  // BackProjectedMisfit): nothing (the per-station contexts), the raw data
+  // of each station (with its rows when the calculator keeps them), or one
+  // station's raw data with identity rows.
+  enum class Serve { kNone, kData, kRows, kUnit };
+
+  // A transform was set through the calculator only: the base class's
+  // GetDataPerMeasurement differs from the raw count and no device
+  // transform was named.
+  bool CalculatorTransformOnly() {
+    return transform_ == J3G_T_NONE && this->GetDataPerMeasurement() != RawDataPerMeasurement();
+  }
+
+  // Calculate with the calculator's transform: the raw data (and rows) of
+  // every station in one device call, then the base class's station loop
+  // over them -- it applies its transform per station and calls
+  // HandleSensitivities in station order (ThreeDGravMagImplementation.h:116-168).
+  rvec ServedCalculate(const ModelType &Model, const DataType &Data,
+                       ThreeDGravMagCalculator<DataType> &Calculator) {
+    const size_t nmeas = Data.GetMeasPosX().size();
+    const size_t raw = RawDataPerMeasurement();
+    const size_t nparm = Model.GetNModelParm();
+    const std::vector<double> params = gb300_detail::to_vector(Model.GetModelParameters());
+    served_.assign(nmeas * raw, 0.0);
+    rmat &cur = Calculator.SetCurrentSensitivities();
+    const bool rows = cur.size1() >= raw && cur.size2() >= nparm;
+    served_rows_.assign(rows ? nmeas * raw * nparm : 0, 0.0);
+    served_nparm_ = nparm;
+    if (nmeas > 0 && rows)
+      Check(ctx_, j3g_forward_sens(ctx_, params.data(), served_.data(), served_rows_.data()),
+            "j3g_forward_sens");
+    else if (nmeas > 0)
+      Check(ctx_, j3g_forward(ctx_, params.data(), served_.data()), "j3g_forward");
+    ServeScope scope(this, rows ? Serve::kRows : Serve::kData);
+    return ThreeDGravMagImplementation<DataType>::Calculate(Model, Data, Calculator);
+  }
+
+  // The raw-length misfit T_i'^T m_i of every station i for a transform set
+  // through the calculator: the raw data from the device, then for each
+  // station the base class's own LQDerivative on a one-station survey and a
+  // model of `raw` parameters whose rows are the identity, which returns
+  // 2 T_i'^T m_i (ThreeDGravMagImplementation.h:177-231).
+  std::vector<double> BackProjectedMisfit(const std::vector<double> &params, const DataType &Data,
+                                          const rvec &Misfit) {
+    const size_t nmeas = Data.GetMeasPosX().size();
+    const size_t raw = RawDataPerMeasurement(), dpm = this->GetDataPerMeasurement();
+    served_.assign(nmeas * raw, 0.0);
+    if (nmeas > 0) Check(ctx_, j3g_forward(ctx_, params.data(), served_.data()), "j3g_forward");
+    ModelType unit;
+    unit.SetMeshSize(raw, 1, 1);
+    if (unit.GetNModelParm() != raw) unit.SetMeshSize(1, 1, 1);  // magnetisation: 3 blocks
+    if (unit.GetNModelParm() != raw)
+      throw FatalException("No model of the raw data size for the transform's derivative",
+                           __FILE__, __LINE__);
+    const std::vector<double> X = gb300_detail::to_vector(Data.GetMeasPosX()),
+                              Y = gb300_detail::to_vector(Data.GetMeasPosY()),
+                              Z = gb300_detail::to_vector(Data.GetMeasPosZ());
+    std::vector<double> out(nmeas * raw);
+    ServeScope scope(this, Serve::kUnit);
+    rvec m(dpm);
+    for (size_t i = 0; i < nmeas; ++i) {
+      DataType one;
+      one.AddMeasurementPoint(X[i], Y[i], Z[i]);
+      for (size_t j = 0; j < dpm; ++j) m(j) = Misfit(i * dpm + j);
+      serve_station_ = i;
+      const rvec g = ThreeDGravMagImplementation<DataType>::LQDerivative(unit, one, m);
+      for (size_t r = 0; r < raw; ++r) out[i * raw + r] = 0.5 * g(r);
+    }
+    return out;
+  }
+
+  struct ServeScope {
+    GB300GravMagImplementation *imp;
+    ServeScope(GB300GravMagImplementation *i, Serve mode) : imp(i) { imp->serve_ = mode; }
+    ~ServeScope() {
+      imp->serve_ = Serve::kNone;
+      imp->served_rows_ = std::vector<double>();
+    }
+  };
+
+  // Per-station parts of the base class's station loops: served from data
+  // computed beforehand (above), or else through a context holding the one
+  // station: the gridded response and rows (columns of the cell blocks), and
+  // the background response and rows (columns ngrid..).
   virtual rvec CalcGridded(const size_t measindex, const ModelType &Model,
                            const DataType &Data, rmat &Sensitivities) override {
+    if (serve_ != Serve::kNone) return Served(measindex, Sensitivities);
     return OneStation(measindex, Model, Data, Sensitivities, true);
   }
   virtual rvec CalcBackground(const size_t measindex, const double, const double,
                               const double, const ModelType &Model, const DataType &Data,
                               rmat &Sensitivities) override {
+    if (serve_ != Serve::kNone) return rvec(RawDataPerMeasurement());  // in the gridded part
     return OneStation(measindex, Model, Data, Sensitivities, false);
+  }
+
+  rvec Served(size_t measindex, rmat &Sens) {
+    const size_t raw = RawDataPerMeasurement();
+    const size_t i = serve_ == Serve::kUnit ? serve_station_ : measindex;
+    rvec out(raw);
+    for (size_t r = 0; r < raw; ++r) out(r) = served_[i * raw + r];
+    if (serve_ == Serve::kUnit) {
+      for (size_t r = 0; r < raw; ++r)
+        for (size_t c = 0; c < Sens.size2(); ++c) Sens(r, c) = r == c ? 1.0 : 0.0;
+    } else if (serve_ == Serve::kRows && Sens.size1() >= raw && Sens.size2() >= served_nparm_) {
+      const double *J = served_rows_.data() + i * raw * served_nparm_;
+      for (size_t r = 0; r < raw; ++r)
+        for (size_t c = 0; c < served_nparm_; ++c) Sens(r, c) = J[r * served_nparm_ + c];
+    }
+    return out;
   }
 
   rvec OneStation(size_t i, const ModelType &Model, const DataType &Data, rmat &Sens,
@@ -308,6 +425,9 @@ class GB300GravMagImplementation : public ThreeDGravMagImplementation<DataType> 
   j3g_context *ctx_ = nullptr;  // all stations
   j3g_context *one_ = nullptr;  // one station (CalcGridded / CalcBackground)
   Geometry main_geo_, one_geo_;
+  Serve serve_ = Serve::kNone;
+  std::vector<double> served_, served_rows_;  // raw data [nmeas][raw], rows [nmeas][raw][nparm]
+  size_t served_nparm_ = 0, serve_station_ = 0;
 };
 
 // Replaces ScalarOMPGravityImp / ScalarCudaGravityImp.

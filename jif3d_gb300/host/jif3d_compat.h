@@ -5,16 +5,21 @@
 // only what the implementation and its tests touch is provided:
 //   rvec / rmat                     (Global/VecMat.h)
 //   FatalException                  (Global/FatalException.h)
-//   VectorTransform + FTGInvariant, TotalField, TotalFieldAnomaly (sizes only)
+//   VectorTransform + FTGInvariant, TotalField, TotalFieldAnomaly (Transform
+//     and Derivative, Gravity/GravityTransforms.h:25-100,
+//     Magnetics/MagneticTransforms.h:19-156)
 //   ThreeDModelBase and the gravity / susceptibility / magnetisation models
 //   the data classes with their ModelType
 //   ThreeDGravMagCalculator, MinMemGravMagCalculator,
 //   FullSensitivityGravMagCalculator (host-stored rows, FP64 products)
-//   ThreeDGravMagImplementation with the generic per-station loop
-//     (GravMag/ThreeDGravMagImplementation.h:116-168), so that the
-//     per-station overrides can be exercised
+//   ThreeDGravMagImplementation with its private transform and the generic
+//     per-station Calculate and LQDerivative loops
+//     (GravMag/ThreeDGravMagImplementation.h:39-231), so that the
+//     per-station overrides and transforms set through a calculator can be
+//     exercised
 #pragma once
 
+#include <cmath>
 #include <memory>
 #include <numeric>
 #include <stdexcept>
@@ -64,26 +69,82 @@ class FatalException : public std::runtime_error {
       : std::runtime_error(what + (file.empty() ? "" : " (" + file + ":" + std::to_string(line) + ")")) {}
 };
 
+// Per-station data transforms: Transform maps the raw data of a station to
+// its transformed data, Derivative gives the output x input Jacobian.
 class VectorTransform {
  public:
   virtual ~VectorTransform() {}
   virtual size_t GetInputSize() const = 0;
   virtual size_t GetOutputSize() const = 0;
+  virtual rvec Transform(const rvec &in) const = 0;
+  virtual rmat Derivative(const rvec &in) const = 0;
 };
+// The second invariant of the tensor Uxx..Uzz (3 x 3, C order).
 class FTGInvariant : public VectorTransform {
  public:
   size_t GetInputSize() const override { return 9; }
   size_t GetOutputSize() const override { return 1; }
+  rvec Transform(const rvec &u) const override {
+    rvec r(1);
+    r(0) = u(0) * u(4) + u(4) * u(8) + u(0) * u(8) - u(3) * u(1) - u(7) * u(5) - u(2) * u(6);
+    return r;
+  }
+  rmat Derivative(const rvec &u) const override {
+    rmat d(1, 9);
+    d(0, 0) = u(4) + u(8);
+    d(0, 1) = -u(3);
+    d(0, 2) = -u(6);
+    d(0, 3) = -u(1);
+    d(0, 4) = u(0) + u(8);
+    d(0, 5) = -u(7);
+    d(0, 6) = -u(2);
+    d(0, 7) = -u(5);
+    d(0, 8) = u(0) + u(4);
+    return d;
+  }
 };
+// |B| of the three components.
 class TotalField : public VectorTransform {
  public:
   size_t GetInputSize() const override { return 3; }
   size_t GetOutputSize() const override { return 1; }
+  rvec Transform(const rvec &b) const override {
+    rvec r(1);
+    r(0) = std::sqrt(b(0) * b(0) + b(1) * b(1) + b(2) * b(2));
+    return r;
+  }
+  rmat Derivative(const rvec &b) const override {
+    const double t = std::sqrt(b(0) * b(0) + b(1) * b(1) + b(2) * b(2));
+    rmat d(1, 3);
+    for (size_t k = 0; k < 3; ++k) d(0, k) = b(k) / t;
+    return d;
+  }
 };
+// The projection of the anomalous field on the inducing field's direction
+// (inclination and declination in radians).
 class TotalFieldAnomaly : public VectorTransform {
  public:
+  explicit TotalFieldAnomaly(double Inclination = 0.0, double Declination = 0.0)
+      : bx_(std::cos(Inclination) * std::cos(Declination)),
+        by_(std::cos(Inclination) * std::sin(Declination)),
+        bz_(std::sin(Inclination)) {}
   size_t GetInputSize() const override { return 3; }
   size_t GetOutputSize() const override { return 1; }
+  rvec Transform(const rvec &b) const override {
+    rvec r(1);
+    r(0) = bx_ * b(0) + by_ * b(1) + bz_ * b(2);
+    return r;
+  }
+  rmat Derivative(const rvec &) const override {
+    rmat d(1, 3);
+    d(0, 0) = bx_;
+    d(0, 1) = by_;
+    d(0, 2) = bz_;
+    return d;
+  }
+
+ private:
+  double bx_, by_, bz_;
 };
 
 // Rectilinear mesh: origin + cell sizes, corner coordinates as running sums
@@ -95,6 +156,16 @@ class ThreeDModelBase {
   typedef std::vector<double> t3DModelDim;
   typedef std::vector<double> t3DModelData;
   virtual ~ThreeDModelBase() {}
+  // cell counts; sizes zero, corners at the origin (ThreeDModelBase.h:146-155)
+  virtual void SetMeshSize(size_t nx, size_t ny, size_t nz) {
+    xs_.assign(nx, 0.0);
+    ys_.assign(ny, 0.0);
+    zs_.assign(nz, 0.0);
+    xc_.assign(nx + 1, 0.0);
+    yc_.assign(ny + 1, 0.0);
+    zc_.assign(nz + 1, 0.0);
+    data_.assign(nx * ny * nz, 0.0);
+  }
   void SetMesh(const std::vector<double> &xs, const std::vector<double> &ys,
                const std::vector<double> &zs, double x0, double y0, double z0) {
     xs_ = xs;
@@ -173,6 +244,11 @@ class ThreeDMagnetizationModel : public ThreeDModelBase {
     return p;
   }
   size_t GetNModelParm() const { return 3 * GetData().size(); }
+  void SetMeshSize(size_t nx, size_t ny, size_t nz) override {
+    ThreeDModelBase::SetMeshSize(nx, ny, nz);
+    my_.assign(nx * ny * nz, 0.0);
+    mz_.assign(nx * ny * nz, 0.0);
+  }
 
  private:
   std::vector<double> my_, mz_;
@@ -283,36 +359,68 @@ class ThreeDGravMagImplementation {
   typedef typename DataType::ModelType ThreeDModelType;
   virtual ~ThreeDGravMagImplementation() {}
   virtual size_t RawDataPerMeasurement() = 0;
+  // not virtual, and the transform is private: a derived class sees only
+  // GetDataPerMeasurement (ThreeDGravMagImplementation.h:44-75)
   void SetDataTransform(std::shared_ptr<VectorTransform> t) { Transform = t; }
   size_t GetDataPerMeasurement() {
     return Transform ? Transform->GetOutputSize() : RawDataPerMeasurement();
   }
-  // The generic station loop: gridded + background per station, then
-  // HandleSensitivities(i).  Without a transform only (stand-in).
+  // The generic station loop (:116-168): gridded + background per station,
+  // the transform applied per station, then HandleSensitivities(i).
   virtual rvec Calculate(const ThreeDModelType &Model, const DataType &Data,
                          ThreeDGravMagCalculator<DataType> &Calculator) {
-    if (Transform)
-      throw FatalException("the stand-in station loop has no data transforms");
     const size_t nmeas = Data.GetMeasPosX().size(), raw = RawDataPerMeasurement();
-    const double xw = std::accumulate(Model.GetXCellSizes().begin(), Model.GetXCellSizes().end(), 0.0);
-    const double yw = std::accumulate(Model.GetYCellSizes().begin(), Model.GetYCellSizes().end(), 0.0);
-    const double zw = std::accumulate(Model.GetZCellSizes().begin(), Model.GetZCellSizes().end(), 0.0);
-    rvec out(nmeas * raw);
+    const size_t dpm = GetDataPerMeasurement();
+    const double xw = Width(Model.GetXCellSizes()), yw = Width(Model.GetYCellSizes()),
+                 zw = Width(Model.GetZCellSizes());
+    rvec out(nmeas * dpm);
     for (size_t i = 0; i < nmeas; ++i) {
-      rvec g = CalcGridded(i, Model, Data, Calculator.SetCurrentSensitivities());
+      rvec cur = CalcGridded(i, Model, Data, Calculator.SetCurrentSensitivities());
       rvec b = CalcBackground(i, xw, yw, zw, Model, Data, Calculator.SetCurrentSensitivities());
-      for (size_t r = 0; r < raw; ++r) out(i * raw + r) = g(r) + b(r);
+      for (size_t r = 0; r < raw; ++r) cur(r) += b(r);
+      const rvec res = Transform ? Transform->Transform(cur) : cur;
+      for (size_t k = 0; k < dpm; ++k) out(i * dpm + k) = res(k);
       Calculator.HandleSensitivities(i);
     }
     return out;
   }
+  // The generic least-squares derivative (:177-231): per station the raw
+  // rows, multiplied by the transform's derivative at the raw data, summed
+  // with the misfit as weights; times 2.
   virtual rvec LQDerivative(const ThreeDModelType &Model, const DataType &Data,
-                            const rvec &Misfit) = 0;
-
- protected:
-  std::shared_ptr<VectorTransform> Transform;
+                            const rvec &Misfit) {
+    const size_t nmeas = Data.GetMeasPosX().size(), raw = RawDataPerMeasurement();
+    const size_t dpm = GetDataPerMeasurement(), nmod = Model.GetNModelParm();
+    if (Misfit.size() != nmeas * dpm) throw FatalException("misfit size");
+    const double xw = Width(Model.GetXCellSizes()), yw = Width(Model.GetYCellSizes()),
+                 zw = Width(Model.GetZCellSizes());
+    rvec deriv(nmod);
+    rmat sens(raw, nmod);
+    for (size_t i = 0; i < nmeas; ++i) {
+      rvec cur = CalcGridded(i, Model, Data, sens);
+      rvec b = CalcBackground(i, xw, yw, zw, Model, Data, sens);
+      for (size_t r = 0; r < raw; ++r) cur(r) += b(r);
+      rmat td(dpm, raw);
+      if (Transform)
+        td = Transform->Derivative(cur);
+      else
+        for (size_t r = 0; r < raw; ++r) td(r, r) = 1.0;
+      for (size_t j = 0; j < dpm; ++j)
+        for (size_t c = 0; c < nmod; ++c) {
+          double v = 0.0;
+          for (size_t r = 0; r < raw; ++r) v += td(j, r) * sens(r, c);
+          deriv(c) += Misfit(i * dpm + j) * v;
+        }
+    }
+    for (size_t c = 0; c < nmod; ++c) deriv(c) *= 2.0;
+    return deriv;
+  }
 
  private:
+  static double Width(const std::vector<double> &v) {
+    return std::accumulate(v.begin(), v.end(), 0.0);
+  }
+  std::shared_ptr<VectorTransform> Transform;
   virtual rvec CalcBackground(const size_t measindex, const double xwidth, const double ywidth,
                               const double zwidth, const ThreeDModelType &Model,
                               const DataType &Data, rmat &Sensitivities) = 0;

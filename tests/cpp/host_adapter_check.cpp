@@ -15,7 +15,10 @@
 //   minmem (MinMem calculator), full (FullSensitivity calculator), rows
 //   (its sensitivity matrix, row-major), grad (LQDerivative), loop (the base
 //   class's per-station loop, no transform only), and "exception ok" when a
-//   wrong misfit size raised FatalException.  Then the device-resident
+//   wrong misfit size raised FatalException; with a transform, the same with
+//   the transform set through the calculators only (a second implementation
+//   object, no SetGB300Transform): calcminmem, calcfull, calcrows, calcgrad
+//   (MinMem) and calcfullgrad (FullSensitivity, first call uncached).  Then the device-resident
 //   calculator (GB300DeviceSensitivityCalculator, fp16 hi / lo storage):
 //   devfirst (first call, FP64), devcached (second call, stored J), devgrad,
 //   devbatch / devbatchgrad (rows k = 0, 1, 2: the model times 1 + 0.1 k and
@@ -98,18 +101,38 @@ void fill(ThreeDMagnetizationModel &m, const Problem &p) {
   m.SetMagnetization_Z().assign(p.model.begin() + 2 * n, p.model.begin() + 3 * n);
 }
 
-std::shared_ptr<VectorTransform> transform_of(int code) {
+std::shared_ptr<VectorTransform> transform_of(int code, double inc, double dec) {
   switch (code) {
     case J3G_T_FTG_INVARIANT: return std::make_shared<FTGInvariant>();
     case J3G_T_TOTAL_FIELD: return std::make_shared<TotalField>();
-    case J3G_T_TFA: return std::make_shared<TotalFieldAnomaly>();
+    case J3G_T_TFA: return std::make_shared<TotalFieldAnomaly>(inc, dec);
     default: return nullptr;
   }
 }
 
+// The transform set through the calculators only, as unchanged jif3D callers
+// do (no SetGB300Transform on this implementation object).
+template <class DataType>
+void run_calculator_transform(const Problem &p,
+                              std::shared_ptr<GB300GravMagImplementation<DataType>> imp,
+                              typename DataType::ModelType &model, const DataType &data,
+                              const rvec &mis, std::FILE *out) {
+  auto t = transform_of(p.transform, p.tinc, p.tdec);
+  if (!t) return;
+  MinMemGravMagCalculator<DataType> minmem(imp);
+  FullSensitivityGravMagCalculator<DataType> full(imp);
+  minmem.SetDataTransform(t);
+  full.SetDataTransform(t);
+  put(out, "calcminmem", minmem.Calculate(model, data));
+  put(out, "calcfull", full.Calculate(model, data));
+  put(out, "calcrows", flatten(full.GetSensitivities()));
+  put(out, "calcgrad", minmem.LQDerivative(model, data, mis));
+  put(out, "calcfullgrad", full.LQDerivative(model, data, mis));
+}
+
 template <class DataType>
 void run(const Problem &p, std::shared_ptr<GB300GravMagImplementation<DataType>> imp,
-         std::FILE *out) {
+         std::shared_ptr<GB300GravMagImplementation<DataType>> plain, std::FILE *out) {
   typename DataType::ModelType model;
   model.SetMesh(p.xs, p.ys, p.zs, p.x0, p.y0, p.z0);
   fill(model, p);
@@ -120,7 +143,7 @@ void run(const Problem &p, std::shared_ptr<GB300GravMagImplementation<DataType>>
 
   MinMemGravMagCalculator<DataType> minmem(imp);
   FullSensitivityGravMagCalculator<DataType> full(imp);
-  if (auto t = transform_of(p.transform)) {
+  if (auto t = transform_of(p.transform, p.tinc, p.tdec)) {
     minmem.SetDataTransform(t);
     full.SetDataTransform(t);
   }
@@ -150,9 +173,10 @@ void run(const Problem &p, std::shared_ptr<GB300GravMagImplementation<DataType>>
   } catch (const FatalException &) {
     std::fprintf(out, "exception ok\n");
   }
+  run_calculator_transform(p, plain, model, data, mis, out);
 
   GB300DeviceSensitivityCalculator<DataType> dev(imp, J3G_STORE_F16X2);
-  if (auto t = transform_of(p.transform)) dev.SetDataTransform(t);
+  if (auto t = transform_of(p.transform, p.tinc, p.tdec)) dev.SetDataTransform(t);
   put(out, "devfirst", dev.Calculate(model, data));
   put(out, "devcached", dev.Calculate(model, data));
   put(out, "devgrad", dev.LQDerivative(model, data, mis));
@@ -175,7 +199,7 @@ void run(const Problem &p, std::shared_ptr<GB300GravMagImplementation<DataType>>
   }
   // the default storage (FP32 J) on the original stations
   GB300DeviceSensitivityCalculator<DataType> dev32(imp);
-  if (auto t = transform_of(p.transform)) dev32.SetDataTransform(t);
+  if (auto t = transform_of(p.transform, p.tinc, p.tdec)) dev32.SetDataTransform(t);
   dev32.Calculate(model, data);  // FP64, builds the FP32 J
   put(out, "dev32cached", dev32.Calculate(model, data));
   put(out, "dev32grad", dev32.LQDerivative(model, data, mis));
@@ -194,21 +218,26 @@ int main(int argc, char **argv) {
     if (!out) return 3;
     switch (p.kind) {
       case J3G_SCALAR:
-        run<ScalarGravityData>(p, std::make_shared<ScalarGB300GravityImp>(), out);
+        run<ScalarGravityData>(p, std::make_shared<ScalarGB300GravityImp>(),
+                               std::make_shared<ScalarGB300GravityImp>(), out);
         break;
       case J3G_TENSOR:
-        run<TensorGravityData>(p, std::make_shared<TensorGB300GravityImp>(), out);
+        run<TensorGravityData>(p, std::make_shared<TensorGB300GravityImp>(),
+                               std::make_shared<TensorGB300GravityImp>(), out);
         break;
       case J3G_MAGNETIC:
         run<TotalFieldMagneticData>(
-            p, std::make_shared<GB300MagneticSusceptibilityImp>(p.inc, p.dec, p.fs), out);
+            p, std::make_shared<GB300MagneticSusceptibilityImp>(p.inc, p.dec, p.fs),
+            std::make_shared<GB300MagneticSusceptibilityImp>(p.inc, p.dec, p.fs), out);
         break;
       case J3G_MAG_GRADIENT:
         run<TotalFieldMagneticData>(p, std::make_shared<GB300MagneticGradImp>(p.inc, p.dec, p.fs),
+                                    std::make_shared<GB300MagneticGradImp>(p.inc, p.dec, p.fs),
                                     out);
         break;
       case J3G_MAGNETIZATION:
-        run<ThreeComponentMagneticData>(p, std::make_shared<GB300MagnetizationImp>(), out);
+        run<ThreeComponentMagneticData>(p, std::make_shared<GB300MagnetizationImp>(),
+                                        std::make_shared<GB300MagnetizationImp>(), out);
         break;
       default:
         std::fprintf(stderr, "unknown kind %d\n", p.kind);

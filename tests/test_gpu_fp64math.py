@@ -35,3 +35,16 @@ def test_fp64_math_accuracy(tmp_path):
         assert rows[name][0] <= 2, (name, rows[name])
     assert rows["specials"][0] == 0, out.stderr
     assert rows["pair"][0] == 0  # fatan2_pair: bit for bit the two separate calls
+
+
+def test_fp64_weight_probe_runs(tmp_path):
+    """The microkernels that the FP64 flop weights are counted on build and
+    run (the counting itself is a profiler capture of this executable)."""
+    exe = str(tmp_path / "fp64_weights_probe")
+    cmd = [B.nvcc(), "-O3", "-std=c++17", B.ARCH, "-I", B.CSRC,
+           os.path.join(HERE, "fp64_weights_probe.cu"), "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.startswith("calls per kernel")

@@ -1,8 +1,9 @@
 """The C++ implementation objects (jif3d_gb300/host/GB300GravMagImplementation.h)
 driven through jif3D-style calculators by tests/cpp/host_adapter_check.cpp:
 MinMem and FullSensitivity calculators, LQDerivative, the base class's
-per-station loop over CalcGridded / CalcBackground, and the FatalException on
-a bad misfit size -- compared with the oracle at the FP64 tolerance (relative
+per-station loop over CalcGridded / CalcBackground, data transforms set through
+the calculators only (as unchanged jif3D callers set them), and the
+FatalException on a bad misfit size -- compared with the oracle at the FP64 tolerance (relative
 norm error <= 1e-10) -- and the device-resident calculator
 (jif3d_gb300/host/GB300DeviceSensitivityCalculator.h): its FP64 first call,
 stored-J calls and batches at the mixed-path tolerance (1e-6), and a moved
@@ -87,6 +88,12 @@ def test_cpp_implementation(oracle_lib, exe, tmp_path, kind, transform):
     if transform == W.T_NONE:  # the per-station loop (stand-in base class, no transform)
         assert relerr(o["loop"], dref) <= TOL
         assert relerr(o["looprows"], Jref.ravel()) <= TOL
+    else:  # the transform set through the calculators only, as unchanged callers do
+        assert relerr(o["calcminmem"], dref) <= TOL
+        assert relerr(o["calcfull"], dref) <= TOL
+        assert relerr(o["calcrows"], Jref.ravel()) <= TOL
+        assert relerr(o["calcgrad"], gref) <= TOL
+        assert relerr(o["calcfullgrad"], gref) <= TOL
     # the device-resident calculator: FP64 first call, then the stored J
     assert relerr(o["devfirst"], dref) <= TOL
     assert relerr(o["devcached"], dref) <= TOL_MIXED

@@ -8,10 +8,13 @@ objective (one ThreeDModelObjective per data set, summed as jif3D's
 JointObjective does with unit weights) over the GPU implementations is
 minimised with scipy's L-BFGS-B for ten iterations, and the same loop runs on
 an objective of the same formulas over the oracle.  The FP64 matrix-free
-calculators must give the oracle's iterates and misfits within 1e-8 relative;
-the device-resident calculator (stored FP32 sensitivities, each product
-within 1e-6 of FP64) within 1e-5, since the iteration carries each
-evaluation's error forward.
+calculators must give the oracle's iterates and misfits within 1e-8 relative.
+The device-resident calculator (stored FP32 sensitivities, each product
+within 1e-6 of FP64) must give the iterates within 1e-5, since the iteration
+carries each evaluation's error forward, and the misfits within 1e-3: chi^2
+sums squares of the data residuals, which are a few per cent of the data
+once the loop has fitted them, so the data's relative error of up to 1e-6 is
+amplified about a hundredfold in it.
 """
 import numpy as np
 import pytest
@@ -110,8 +113,8 @@ def lbfgs(fun, m0):
     return np.array(xs), np.array(fs)
 
 
-@pytest.mark.parametrize("calc,tol", [("minmem", 1e-8), ("device", 1e-5)])
-def test_lbfgs_iterates_match_oracle(oracle_lib, calc, tol):
+@pytest.mark.parametrize("calc,tol,ftol", [("minmem", 1e-8, 1e-8), ("device", 1e-5, 1e-3)])
+def test_lbfgs_iterates_match_oracle(oracle_lib, calc, tol, ftol):
     pytest.importorskip("scipy")
     s, t, obs = survey_and_data(oracle_lib)
     m0 = s.model.copy()
@@ -125,4 +128,4 @@ def test_lbfgs_iterates_match_oracle(oracle_lib, calc, tol):
     for k in range(ITERATIONS):
         ex = np.linalg.norm(x_gpu[k] - x_ref[k]) / np.linalg.norm(x_ref[k])
         ef = abs(f_gpu[k] - f_ref[k]) / f_ref[k]
-        assert ex <= tol and ef <= tol, (k, ex, ef)
+        assert ex <= tol and ef <= ftol, (k, ex, ef)
