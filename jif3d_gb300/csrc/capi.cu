@@ -960,25 +960,15 @@ int batched_adjoint_pass(j3g_context *c, int nmod, const double *d_models,
     J3G_TRY(gemm_plan(c, 1, g, K, slice, plan));
     c->last_plan[1] = plan;
     const int nsp = gemm_splits_used(ldR, plan.nsplit);
-    if (gemm_fused2_ok(g, plan.nsplit, plan.tile)) {
-      // two splits on CTA pairs: the split sum in the product's epilogue
-      // (the same values as the product + split-sum launches below), out =
-      // 2 * modscale[n] * (P0 + P1)
+    {
       TimedScope ts(c, J3G_TIMER_GEMM_ADJOINT);
-      J3G_LAUNCH(c, launch_gemm_x3_fused2(g, plan.nsplit, ptr<float>(c->P), K, d_grads, np,
-                                          ptr<float>(c->mscale), 1, ptr<int>(c->gerr),
-                                          c->stream, plan.tile));
-    } else {
-      {
-        TimedScope ts(c, J3G_TIMER_GEMM_ADJOINT);
-        J3G_LAUNCH(c, launch_gemm_x3(g, plan.nsplit, ptr<float>(c->P), K, slice,
-                                     ptr<int>(c->gerr), c->stream, plan.tile));
-      }
-      TimedScope ts(c, J3G_TIMER_REDUCE);
-      J3G_LAUNCH(c, launch_splitk_reduce(ptr<float>(c->P), nsp, slice, nmod, (int)K, K, nullptr,
-                                         ptr<float>(c->mscale), nullptr, nullptr, 2.0, d_grads,
-                                         np, c->stream));
+      J3G_LAUNCH(c, launch_gemm_x3(g, plan.nsplit, ptr<float>(c->P), K, slice,
+                                   ptr<int>(c->gerr), c->stream, plan.tile));
     }
+    TimedScope ts(c, J3G_TIMER_REDUCE);
+    J3G_LAUNCH(c, launch_splitk_reduce(ptr<float>(c->P), nsp, slice, nmod, (int)K, K, nullptr,
+                                       ptr<float>(c->mscale), nullptr, nullptr, 2.0, d_grads, np,
+                                       c->stream));
   }
   if (nbg) {
     TimedScope ts(c, J3G_TIMER_EPILOGUE);

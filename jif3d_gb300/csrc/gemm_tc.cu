@@ -34,7 +34,6 @@
 #include <set>
 #include <utility>
 
-#include "fpbits.cuh"
 #include "stored.h"
 
 namespace j3g {
@@ -511,29 +510,14 @@ __device__ __forceinline__ void umma_commit_pair_local(uint32_t bar) {
                : "memory");
 }
 
-// FUSE2: the pair runs both halves of a two-split K range itself.  At the
-// start of the second half its drain warps store the first half's FP32 sums
-// in P (split 0's slice) and start again from zero; at the end each thread
-// reads back its own stored values, adds them to the second half's sums
-// (one round-to-nearest FP32 add: the value the split-sum pass gives for two
-// splits) and writes the final FP64 results, scaled by the power of two
-// 2^(pow2_exponent(modscale[n]) + kfac), to out[n * ld_out + row] -- no
-// separate reduction launch, the partials written and read once.
-struct FusedOut {
-  double *out;
-  long long ld_out;
-  const float *modscale;  // per model, a power of two (may be null)
-  int kfac;               // the product's factor, 2^kfac
-};
-
-template <bool F16, bool FUSE2>
+template <bool F16>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
     k_gemm_pair(const __grid_constant__ CUtensorMap tmAhi,
                 const __grid_constant__ CUtensorMap tmAlo,
                 const __grid_constant__ CUtensorMap tmBhi,
                 const __grid_constant__ CUtensorMap tmBlo, int kb_per_split, int kb_total, int M,
                 int N, float *__restrict__ P, long long ldp, long long slice,
-                int *__restrict__ err, int fault, FusedOut fo) {
+                int *__restrict__ err, int fault) {
   using C = PairCfg<F16>;
   constexpr int S = C::STAGES;
   extern __shared__ uint8_t smem_raw[];
@@ -551,7 +535,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
   const int n0 = blockIdx.y * kPairN;                       // the pair's models
   const int nb0 = n0 + (int)rank * (kPairN / 2);            // this CTA's rows of B
   const int kb0 = blockIdx.z * kb_per_split;
-  const int nkb = FUSE2 ? kb_total : min(kb_total, kb0 + kb_per_split) - kb0;
+  const int nkb = min(kb_total, kb0 + kb_per_split) - kb0;
   const int ndrain = nkb * kDrainsPerBlock;
 
   if (threadIdx.x == 0) {
@@ -677,20 +661,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
     float s[C::COLS_PER_WARP];
 #pragma unroll
     for (int j = 0; j < C::COLS_PER_WARP; ++j) s[j] = 0.0f;
-    const int row = m0 + q * 32 + lane;
-    // FUSE2: the first drain of the second half (split 0 is the first
-    // kb_per_split k-blocks, as in the two-split plan)
-    const int d_half = FUSE2 ? min(kb_per_split * kDrainsPerBlock, ndrain) : ndrain;
-    // one drain: wait for accumulator d, add it into the sums, release it;
-    // false when the wait expired
-    auto drain = [&](int d) -> bool {
+    for (int d = 0; d < ndrain; ++d) {
       const int b = d % kPairAcc;
       // the lanes decide together: tcgen05.ld below is warp-collective
       const bool got =
           __all_sync(0xffffffffu, mbar_wait(smem_u32(a_full + b), (uint32_t)(d / kPairAcc) & 1u));
       if (!got) {
         if (lane == 0) atomicExch(err, 4);
-        return false;
+        break;
       }
       tc_fence_after();
       const uint32_t acc = tmem + (uint32_t)(b * kPairN) + lane_off + col0;
@@ -717,61 +695,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kPairThreads, 1)
         else
           mbar_arrive_remote(peer_addr(smem_u32(a_empty + b), 0));
       }
-      return true;
-    };
-    bool ok = true;
-    for (int d = 0; d < d_half && ok; ++d) ok = drain(d);
-    if (FUSE2 && ok) {
-      // the first half's sums go to P; the second half starts from zero
-      if (row < M) {
-        const int nv = min(C::COLS_PER_WARP, N - (n0 + (int)col0));
-        float *pp = P + (long long)(n0 + (int)col0) * ldp + row;
-#pragma unroll
-        for (int j = 0; j < C::COLS_PER_WARP; ++j) {
-          if (j < nv) *pp = s[j];
-          pp += ldp;
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < C::COLS_PER_WARP; ++j) s[j] = 0.0f;
-      for (int d = d_half; d < ndrain && ok; ++d) ok = drain(d);
     }
-    if (FUSE2) {
-      if (ok && row < M) {
-        // the thread's own stores of the first half, read back in order
-        const int nv = min(C::COLS_PER_WARP, N - (n0 + (int)col0));
-        const float *pp = P + (long long)(n0 + (int)col0) * ldp + row;
-        double *oo = fo.out + (long long)(n0 + (int)col0) * fo.ld_out + row;
-        const float *ms = fo.modscale ? fo.modscale + n0 + (int)col0 : nullptr;
-        // groups of 16 values; the compiler barrier between groups keeps
-        // the loads of later groups from being hoisted into this one's
-        // registers (the 64 sums already take most of them)
+    const int row = m0 + q * 32 + lane;
+    float *out = P + (long long)blockIdx.z * slice;
+    if (row < M) {
 #pragma unroll
-        for (int g = 0; g < C::COLS_PER_WARP; g += 16) {
-          float p[16];
-#pragma unroll
-          for (int i = 0; i < 16; ++i) p[i] = g + i < nv ? pp[(long long)i * ldp] : 0.0f;
-#pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            if (g + i < nv) {
-              const float v = __fadd_rn(p[i], s[g + i]);
-              const int k = (ms ? pow2_exponent(ms[g + i]) : 0) + fo.kfac;
-              oo[(long long)i * fo.ld_out] = scale_pow2(f32_to_f64(v), k);
-            }
-          }
-          pp += 16 * ldp;
-          oo += 16 * fo.ld_out;
-          asm volatile("" ::: "memory");
-        }
-      }
-    } else {
-      float *out = P + (long long)blockIdx.z * slice;
-      if (row < M) {
-#pragma unroll
-        for (int j = 0; j < C::COLS_PER_WARP; ++j) {
-          const int n = n0 + (int)col0 + j;
-          if (n < N) out[(long long)n * ldp + row] = s[j];
-        }
+      for (int j = 0; j < C::COLS_PER_WARP; ++j) {
+        const int n = n0 + (int)col0 + j;
+        if (n < N) out[(long long)n * ldp + row] = s[j];
       }
     }
   }
@@ -874,9 +805,9 @@ cudaError_t launch_bn(const GemmOperands &g, int nsplit, float *P, long long ldp
   return cudaGetLastError();
 }
 
-template <bool F16, bool FUSE2>
+template <bool F16>
 cudaError_t launch_pair(const GemmOperands &g, int nsplit, float *P, long long ldp,
-                        long long slice, int *err, cudaStream_t st, const FusedOut &fo) {
+                        long long slice, int *err, cudaStream_t st) {
   CUtensorMap ah, al, bh, bl;
   if (!make_tiled_map(&ah, g.a_hi, g.m, g.ld, F16) || !make_tiled_map(&al, g.a_lo, g.m, g.ld, F16) ||
       !make_map(&bh, g.b_hi, g.n_pad, g.ld, kPairN / 2, F16) ||
@@ -885,16 +816,13 @@ cudaError_t launch_pair(const GemmOperands &g, int nsplit, float *P, long long l
   const int kb_total = (int)(g.ld / BK);
   const int kb_per = (kb_total + nsplit - 1) / nsplit;
   const int nsp = (kb_total + kb_per - 1) / kb_per;
-  if (FUSE2 && nsp != 2) return cudaErrorInvalidValue;
-  cudaError_t e = allow_smem_once(reinterpret_cast<const void *>(k_gemm_pair<F16, FUSE2>),
+  cudaError_t e = allow_smem_once(reinterpret_cast<const void *>(k_gemm_pair<F16>),
                                   PairCfg<F16>::SMEM);
   if (e != cudaSuccess) return e;
-  // x: CTA pairs over M (two CTAs of 128 rows each), y: N tiles of 256, z: K
-  // splits (FUSE2: one z, both splits in each pair)
-  dim3 grid((unsigned)(2 * ((g.m + 255) / 256)), (unsigned)(g.n_pad / kPairN),
-            FUSE2 ? 1u : (unsigned)nsp);
-  k_gemm_pair<F16, FUSE2><<<grid, kPairThreads, PairCfg<F16>::SMEM, st>>>(
-      ah, al, bh, bl, kb_per, kb_total, (int)g.m, (int)g.n, P, ldp, slice, err, g.fault, fo);
+  // x: CTA pairs over M (two CTAs of 128 rows each), y: N tiles of 256, z: K splits
+  dim3 grid((unsigned)(2 * ((g.m + 255) / 256)), (unsigned)(g.n_pad / kPairN), (unsigned)nsp);
+  k_gemm_pair<F16><<<grid, kPairThreads, PairCfg<F16>::SMEM, st>>>(
+      ah, al, bh, bl, kb_per, kb_total, (int)g.m, (int)g.n, P, ldp, slice, err, g.fault);
   return cudaGetLastError();
 }
 
@@ -917,32 +845,14 @@ cudaError_t launch_gemm_x3(const GemmOperands &g, int nsplit, float *P, long lon
   if ((reinterpret_cast<uintptr_t>(g.a_hi) | reinterpret_cast<uintptr_t>(g.a_lo) |
        reinterpret_cast<uintptr_t>(g.b_hi) | reinterpret_cast<uintptr_t>(g.b_lo)) & 15)
     return cudaErrorMisalignedAddress;
-  const FusedOut none{nullptr, 0, nullptr, 0};
   if (g.f16) {
-    if (nt == kPairN) return launch_pair<true, false>(g, nsplit, P, ldp, slice, err, st, none);
+    if (nt == kPairN) return launch_pair<true>(g, nsplit, P, ldp, slice, err, st);
     if (nt == 64) return launch_bn<64, true>(g, nsplit, P, ldp, slice, err, st);
     return launch_bn<128, true>(g, nsplit, P, ldp, slice, err, st);
   }
-  if (nt == kPairN) return launch_pair<false, false>(g, nsplit, P, ldp, slice, err, st, none);
+  if (nt == kPairN) return launch_pair<false>(g, nsplit, P, ldp, slice, err, st);
   if (nt == 64) return launch_bn<64, false>(g, nsplit, P, ldp, slice, err, st);
   return launch_bn<128, false>(g, nsplit, P, ldp, slice, err, st);
-}
-
-bool gemm_fused2_ok(const GemmOperands &g, int nsplit, int tile) {
-  const int nt = tile ? tile : gemm_n_tile((int)g.n);
-  return g.f16 && nt == kPairN && g.ld % BK == 0 && g.n_pad % kPairN == 0 &&
-         gemm_splits_used(g.ld, nsplit) == 2;
-}
-
-cudaError_t launch_gemm_x3_fused2(const GemmOperands &g, int nsplit, float *P, long long ldp,
-                                  double *out, long long ld_out, const float *modscale, int kfac,
-                                  int *err, cudaStream_t st, int tile) {
-  if (!gemm_fused2_ok(g, nsplit, tile)) return cudaErrorInvalidValue;
-  if ((reinterpret_cast<uintptr_t>(g.a_hi) | reinterpret_cast<uintptr_t>(g.a_lo) |
-       reinterpret_cast<uintptr_t>(g.b_hi) | reinterpret_cast<uintptr_t>(g.b_lo)) & 15)
-    return cudaErrorMisalignedAddress;
-  const FusedOut fo{out, ld_out, modscale, kfac};
-  return launch_pair<true, true>(g, nsplit, P, ldp, 0, err, st, fo);
 }
 
 }  // namespace j3g

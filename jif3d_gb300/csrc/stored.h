@@ -99,15 +99,5 @@ int gemm_splits_used(long long ld, int nsplit);
 // the CTA-pair kernel (n_pad must be a multiple of the tile).
 cudaError_t launch_gemm_x3(const GemmOperands &g, int nsplit, float *P, long long ldp,
                            long long slice, int *err, cudaStream_t st, int tile = 0);
-// A plan of exactly two K splits on CTA pairs (fp16 operands) can run with
-// the split sum fused in: each pair computes both splits, and
-// out[n * ld_out + r] = 2^(pow2_exponent(modscale[n]) + kfac) * fl32(P0 + P1)
-// -- the values of launch_gemm_x3 followed by launch_splitk_reduce with
-// factor 2^kfac, without the separate reduction (P holds split 0's sums
-// between the two halves).
-bool gemm_fused2_ok(const GemmOperands &g, int nsplit, int tile);
-cudaError_t launch_gemm_x3_fused2(const GemmOperands &g, int nsplit, float *P, long long ldp,
-                                  double *out, long long ld_out, const float *modscale, int kfac,
-                                  int *err, cudaStream_t st, int tile = 0);
 
 }  // namespace j3g
