@@ -169,54 +169,68 @@ __device__ void tensor_box9(double mx, double my, double mz, double cx, double c
   u[7] = u[5];
 }
 
-__global__ void k_background(int kind, StationView st, int nbg, const double *__restrict__ thick,
-                             double xo, double yo, double zo, double xw, double yw, double zw,
-                             MagField mf, double *__restrict__ bgsens) {
+// Background layer terms (GravityBackground.cpp:24-137): one thread per
+// (station, layer) -- the layers of a station are independent once the
+// layer's top is known, which each thread sums from the thicknesses in layer
+// order, as the reference's loop does -- with the kind a template argument so
+// that the term arrays stay in registers.  Small blocks spread the few
+// hundred to few thousand threads of a survey over many SMs.
+template <int KIND>
+__global__ void __launch_bounds__(32) k_background(StationView st, int nbg,
+                                                   const double *__restrict__ thick, double xo,
+                                                   double yo, double zo, double xw, double yw,
+                                                   double zw, MagField mf,
+                                                   double *__restrict__ bgsens) {
+  constexpr int kind = KIND;
+  constexpr int raw = kind_raw(kind);
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= st.n) return;
-  const int raw = kind_raw(kind);
-  if (kind_special(kind)) {  // no background response (OMPMagneticGradImp.h:32-40)
-    for (int r = 0; r < raw; ++r)
-      for (int j = 0; j < nbg; ++j) bgsens[((long long)s * raw + r) * nbg + j] = 0.0;
+  const int j = blockIdx.y;
+  if (s >= st.n || j >= nbg) return;
+  if constexpr (kind_special(kind)) {  // no background response (OMPMagneticGradImp.h:32-40)
+#pragma unroll
+    for (int r = 0; r < raw; ++r) bgsens[((long long)s * raw + r) * nbg + j] = 0.0;
     return;
-  }
-  const double mx = st.x[s], my = st.y[s], mz = st.z[s];
-  double top = zo;
-  for (int j = 0; j < nbg; ++j) {
+  } else {
+    const double mx = st.x[s], my = st.y[s], mz = st.z[s];
+    double top = zo;
+    for (int i = 0; i < j; ++i) top = add(top, thick[i]);
     const double th = thick[j];
     const double bottom = add(top, th);
-    double v[10];
-    if (kind == KIND_SCALAR || kind == KIND_JOINT) {
+    double v[raw];
+    if constexpr (kind == KIND_SCALAR || kind == KIND_JOINT) {
       double g = inf_sheet(mz, top, bottom);
       if (top < zw && (bottom <= zw)) g = sub(g, grav_box(mx, my, mz, xo, yo, top, xw, yw, th));
       if (top < zw && bottom > zw)
         g = sub(g, grav_box(mx, my, mz, xo, yo, top, xw, yw, sub(zw, top)));
       v[0] = g;
     }
-    if (kind != KIND_SCALAR) {
+    if constexpr (kind != KIND_SCALAR) {
       double u[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
       double b[9];
       u[8] = uzz_inf_sheet(mz, top, bottom);
       if (top < zw && (bottom <= zw)) {
         tensor_box9(mx, my, mz, xo, yo, top, xw, yw, th, b);
+#pragma unroll
         for (int c = 0; c < 9; ++c) u[c] = sub(u[c], b[c]);
       }
       if (top < zw && bottom > zw) {
         tensor_box9(mx, my, mz, xo, yo, top, xw, yw, sub(zw, top), b);
+#pragma unroll
         for (int c = 0; c < 9; ++c) u[c] = sub(u[c], b[c]);
       }
-      if (kind == KIND_MAGNETIC) {
+      if constexpr (kind == KIND_MAGNETIC) {
         const double f1 = mf.fs, f2 = mf.factor;
         v[0] = mul(mul(add(add(mul(u[0], mf.bx), mul(u[1], mf.by)), mul(u[2], mf.bz)), f1), f2);
         v[1] = mul(mul(add(add(mul(u[3], mf.bx), mul(u[4], mf.by)), mul(u[5], mf.bz)), f1), f2);
         v[2] = mul(mul(add(add(mul(u[6], mf.bx), mul(u[7], mf.by)), mul(u[8], mf.bz)), f1), f2);
       } else {
-        double *t = (kind == KIND_JOINT) ? v + 1 : v;
-        for (int c = 0; c < 9; ++c) t[c] = u[c];
+        constexpr int o = kind == KIND_JOINT ? 1 : 0;
+#pragma unroll
+        for (int c = 0; c < 9; ++c) v[o + c] = u[c];
       }
     }
+#pragma unroll
     for (int r = 0; r < raw; ++r) bgsens[((long long)s * raw + r) * nbg + j] = v[r];
-    top = add(top, th);
   }
 }
 
@@ -708,9 +722,11 @@ cudaError_t launch_background(int kind, const MeshView &m, const StationView &s,
                               double yw, double zw, const MagField &mf, double *bgsens,
                               cudaStream_t st) {
   (void)m;
-  if (nbg == 0) return cudaSuccess;
-  k_background<<<cdiv(s.n, 128), 128, 0, st>>>(kind, s, nbg, bg_thick, xo, yo, zo, xw, yw, zw,
-                                                 mf, bgsens);
+  if (nbg == 0 || s.n == 0) return cudaSuccess;
+  if (nbg > 65535) return cudaErrorInvalidValue;
+  const dim3 grid(cdiv(s.n, 32), nbg);
+  J3G_DISPATCH(kind, (k_background<K><<<grid, 32, 0, st>>>(s, nbg, bg_thick, xo, yo, zo, xw, yw,
+                                                             zw, mf, bgsens)));
   return cudaGetLastError();
 }
 
