@@ -100,6 +100,26 @@ def test_non_running_sum_coordinates_use_corner_path(ctx, oracle_lib, kind):
     assert relerr(c.lqderivative(s.model, misfit), p.lqderivative(s.model, misfit)) <= TOL
 
 
+@pytest.mark.parametrize("kind", KINDS)
+def test_many_background_layers(ctx, oracle_lib, kind):
+    """Forty background layers (one thread per station and layer), some
+    inside the gridded depth, some across its bottom and some below it, with
+    80 stations (several thread blocks): data and gradient, background
+    columns included, against the oracle."""
+    s = small_survey(kind, seed=95 + kind, nmeas=80)
+    rng = np.random.default_rng(kind)
+    s.bg_thick = rng.uniform(5.0, 60.0, 40)
+    s.model = np.concatenate([s.model[:s.ngrid], rng.uniform(1, 5, 40)])
+    c = gpu(ctx, s)
+    d = c.forward(s.model)
+    assert relerr(d, oracle_forward(oracle_lib, s)) <= TOL
+    misfit = rng.normal(size=d.size)
+    g = c.lqderivative(s.model, misfit)
+    gref = oracle_lqderivative(oracle_lib, s, misfit)
+    assert relerr(g, gref) <= TOL
+    assert relerr(g[s.ngrid:], gref[s.ngrid:]) <= TOL
+
+
 def test_edge_cases(ctx, oracle_lib):
     O = oracle_lib
     # background only, no grid cells (test_ScalarCalculation.cpp:123-147)
