@@ -169,54 +169,77 @@ __device__ void tensor_box9(double mx, double my, double mz, double cx, double c
   u[7] = u[5];
 }
 
-// Background layer terms (GravityBackground.cpp:24-137): one thread per
-// (station, layer) -- the layers of a station are independent once the
-// layer's top is known, which each thread sums from the thicknesses in layer
-// order, as the reference's loop does -- with the kind a template argument so
-// that the term arrays stay in registers.  Small blocks spread the few
-// hundred to few thousand threads of a survey over many SMs.
+// Background layer terms (GravityBackground.cpp:24-137).  A block takes 32
+// stations of one layer; warp k evaluates one prism component (g_z, Uxx, Uyy,
+// Uzz, Uxy, Uxz, Uyz; the eighth warp idles) for those 32 stations, each an
+// eight-corner sum in the reference's order, so the serial chain of
+// transcendentals per thread is one component long and no warp diverges.
+// Warp 0 then combines them with the sheet terms exactly as the reference's
+// per-station loop does.  A layer's top is summed from the
+// thicknesses in layer order.  The kind is a template argument so that the
+// term arrays stay in registers.
 template <int KIND>
-__global__ void __launch_bounds__(32) k_background(StationView st, int nbg,
-                                                   const double *__restrict__ thick, double xo,
-                                                   double yo, double zo, double xw, double yw,
-                                                   double zw, MagField mf,
-                                                   double *__restrict__ bgsens) {
+__global__ void __launch_bounds__(256) k_background(StationView st, int nbg,
+                                                    const double *__restrict__ thick, double xo,
+                                                    double yo, double zo, double xw, double yw,
+                                                    double zw, MagField mf,
+                                                    double *__restrict__ bgsens) {
   constexpr int kind = KIND;
   constexpr int raw = kind_raw(kind);
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int slot = threadIdx.x >> 5, li = threadIdx.x & 31;  // component, station
+  const int s = blockIdx.x * 32 + li;
   const int j = blockIdx.y;
-  if (s >= st.n || j >= nbg) return;
+  const bool live = s < st.n;
   if constexpr (kind_special(kind)) {  // no background response (OMPMagneticGradImp.h:32-40)
-#pragma unroll
-    for (int r = 0; r < raw; ++r) bgsens[((long long)s * raw + r) * nbg + j] = 0.0;
+    if (live && slot < raw) bgsens[((long long)s * raw + slot) * nbg + j] = 0.0;
     return;
   } else {
-    const double mx = st.x[s], my = st.y[s], mz = st.z[s];
+    __shared__ double terms[32][8];
+    double mx = 0.0, my = 0.0, mz = 0.0;
+    if (live) {
+      mx = st.x[s];
+      my = st.y[s];
+      mz = st.z[s];
+    }
     double top = zo;
     for (int i = 0; i < j; ++i) top = add(top, thick[i]);
     const double th = thick[j];
     const double bottom = add(top, th);
+    // the slab inside the gridded depth, whole or cut at its bottom
+    const bool have = top < zw;
+    const double h = bottom <= zw ? th : sub(zw, top);
+    constexpr bool kGz = kind == KIND_SCALAR || kind == KIND_JOINT;
+    constexpr bool kTensor = kind != KIND_SCALAR;
+    double b = 0.0;
+    if (live && have) {
+      if (slot == 0 && kGz) b = grav_box(mx, my, mz, xo, yo, top, xw, yw, h);
+      if (kTensor) {
+        if (slot == 1) b = uxx_box(mx, my, mz, xo, yo, top, xw, yw, h);
+        if (slot == 2) b = uxx_box(my, mx, mz, yo, xo, top, yw, xw, h);
+        if (slot == 3) b = uxx_box(mz, mx, my, top, xo, yo, h, xw, yw);
+        if (slot == 4) b = uxy_box(mx, my, mz, xo, yo, top, xw, yw, h);
+        if (slot == 5) b = uxy_box(mx, mz, my, xo, top, yo, xw, h, yw);
+        if (slot == 6) b = uxy_box(mz, my, mx, top, yo, xo, h, yw, xw);
+      }
+    }
+    terms[li][slot] = b;
+    __syncthreads();
+    if (!live || slot != 0) return;
+    const double *t = terms[li];
     double v[raw];
-    if constexpr (kind == KIND_SCALAR || kind == KIND_JOINT) {
+    if constexpr (kGz) {
       double g = inf_sheet(mz, top, bottom);
-      if (top < zw && (bottom <= zw)) g = sub(g, grav_box(mx, my, mz, xo, yo, top, xw, yw, th));
-      if (top < zw && bottom > zw)
-        g = sub(g, grav_box(mx, my, mz, xo, yo, top, xw, yw, sub(zw, top)));
+      if (have) g = sub(g, t[0]);
       v[0] = g;
     }
-    if constexpr (kind != KIND_SCALAR) {
+    if constexpr (kTensor) {
+      // 3 x 3 tensor from the unique components (BasicGravElements.cpp:216-244)
+      const double box[9] = {t[1], t[4], t[5], t[4], t[2], t[6], t[5], t[6], t[3]};
       double u[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-      double b[9];
       u[8] = uzz_inf_sheet(mz, top, bottom);
-      if (top < zw && (bottom <= zw)) {
-        tensor_box9(mx, my, mz, xo, yo, top, xw, yw, th, b);
+      if (have) {
 #pragma unroll
-        for (int c = 0; c < 9; ++c) u[c] = sub(u[c], b[c]);
-      }
-      if (top < zw && bottom > zw) {
-        tensor_box9(mx, my, mz, xo, yo, top, xw, yw, sub(zw, top), b);
-#pragma unroll
-        for (int c = 0; c < 9; ++c) u[c] = sub(u[c], b[c]);
+        for (int c = 0; c < 9; ++c) u[c] = sub(u[c], box[c]);
       }
       if constexpr (kind == KIND_MAGNETIC) {
         const double f1 = mf.fs, f2 = mf.factor;
@@ -725,8 +748,8 @@ cudaError_t launch_background(int kind, const MeshView &m, const StationView &s,
   if (nbg == 0 || s.n == 0) return cudaSuccess;
   if (nbg > 65535) return cudaErrorInvalidValue;
   const dim3 grid(cdiv(s.n, 32), nbg);
-  J3G_DISPATCH(kind, (k_background<K><<<grid, 32, 0, st>>>(s, nbg, bg_thick, xo, yo, zo, xw, yw,
-                                                             zw, mf, bgsens)));
+  J3G_DISPATCH(kind, (k_background<K><<<grid, 256, 0, st>>>(s, nbg, bg_thick, xo, yo, zo, xw, yw,
+                                                              zw, mf, bgsens)));
   return cudaGetLastError();
 }
 
