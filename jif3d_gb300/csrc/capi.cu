@@ -921,8 +921,13 @@ int batched_adjoint_pass(j3g_context *c, int nmod, const double *d_models,
     rawd = ptr<double>(c->rawb);
   }
   J3G_TRY(ensure(c, c->wrawb, sizeof(double) * (size_t)nmod * c->nmeas * raw));
-  J3G_TRY(ensure(c, c->wst, sizeof(double) * (size_t)nmod * R));
-  {
+  const int tile = gemm_n_tile(nmod);
+  const long long npad = (nmod + tile - 1) / tile * tile;
+  // fp16 products on a survey that fits one block per model: the weights and
+  // their split in one launch (the same values as the two launches below)
+  const bool fused = c->storage != J3G_STORE_FP32 && weights_split_fits(c->nmeas, ldR, (int)npad);
+  if (!fused) {
+    J3G_TRY(ensure(c, c->wst, sizeof(double) * (size_t)nmod * R));
     TimedScope ts(c, J3G_TIMER_EPILOGUE);
     J3G_LAUNCH(c, launch_stored_weights(c->kind, c->transform, tbx, tby, tbz, c->nmeas, nmod,
                                         d_misfits, (long long)c->nmeas * c->dpm(), rawd,
@@ -938,14 +943,19 @@ int batched_adjoint_pass(j3g_context *c, int nmod, const double *d_models,
       ++c->launches;
     }
   } else {
-    const int tile = gemm_n_tile(nmod);
-    const long long npad = (nmod + tile - 1) / tile * tile;
     J3G_TRY(ensure(c, c->Bhi, 2 * (size_t)npad * std::max(ldR, ldK)));
     J3G_TRY(ensure(c, c->Blo, 2 * (size_t)npad * std::max(ldR, ldK)));
     J3G_TRY(ensure(c, c->mscale, sizeof(float) * (size_t)npad));
-    J3G_TRY(ensure(c, c->swork, sizeof(double) * (size_t)split_matrix_work((int)npad, ldR)));
     // residual weights carry the row scale of J: J = s_r (hi + lo)
-    {
+    if (fused) {
+      TimedScope ts(c, J3G_TIMER_SPLIT);
+      J3G_LAUNCH(c, launch_weights_split(c->kind, c->transform, tbx, tby, tbz, c->nmeas, nmod,
+                                         (int)npad, d_misfits, (long long)c->nmeas * c->dpm(),
+                                         rawd, mag_field(c), ptr<double>(c->wrawb),
+                                         ptr<float>(c->rowscale), ptr<float>(c->mscale),
+                                         c->Bhi.p, c->Blo.p, ldR, c->stream));
+    } else {
+      J3G_TRY(ensure(c, c->swork, sizeof(double) * (size_t)split_matrix_work((int)npad, ldR)));
       TimedScope ts(c, J3G_TIMER_SPLIT);
       J3G_LAUNCH(c, launch_split_matrix(ptr<double>(c->wst), R, nmod, R, ptr<float>(c->rowscale),
                                         c->Bhi.p, c->Blo.p, ldR, (int)npad, ptr<float>(c->mscale),

@@ -626,6 +626,46 @@ k_stored_assemble(int transform, double tbx, double tby, double tbz, int nmeas,
     }
   }
 }
+// Raw-row weights of one station: the misfit back-projected through the
+// transform's derivative at the station's raw data d (Gravity/GravityTransforms.h:
+// 72-93, Magnetics/MagneticTransforms.h:65-75, 136-145); w = the misfit
+// itself without a transform.
+template <int RAW>
+__device__ __forceinline__ void station_weights(int transform, double tbx, double tby,
+                                                double tbz, const double *mis_raw, double m,
+                                                const double *d, double *w) {
+  if (transform == TR_NONE) {
+#pragma unroll
+    for (int c = 0; c < RAW; ++c) w[c] = mis_raw[c];
+  } else if (transform == TR_FTG_INVARIANT) {
+    w[0] = mul(m, add(d[4], d[8])); w[1] = mul(m, -d[3]); w[2] = mul(m, -d[6]);
+    w[3] = mul(m, -d[1]); w[4] = mul(m, add(d[0], d[8])); w[5] = mul(m, -d[7]);
+    w[6] = mul(m, -d[2]); w[7] = mul(m, -d[5]); w[8] = mul(m, add(d[0], d[4]));
+  } else if (transform == TR_TOTAL_FIELD) {
+    const double tt = sqrt(add(add(mul(d[0], d[0]), mul(d[1], d[1])), mul(d[2], d[2])));
+    for (int c = 0; c < 3; ++c) w[c] = mul(m, d[c] / tt);
+  } else {
+    w[0] = mul(m, tbx); w[1] = mul(m, tby); w[2] = mul(m, tbz);
+  }
+}
+
+// Stored-row weights of one station from its raw-row weights.
+template <int KIND>
+__device__ __forceinline__ void stored_weights(const double *w, const MagField &mf, double *st) {
+  constexpr int kind = KIND;
+  constexpr int raw = kind_raw(kind);
+  constexpr int ns = stored_rows(kind);
+  if constexpr (stored_is_raw(kind)) {
+#pragma unroll
+    for (int c = 0; c < raw; ++c) st[c] = w[c];
+  } else {
+    double u[NC_COUNT];
+    comps_from_raw_weights(kind, w, mf, u);
+#pragma unroll
+    for (int q = 0; q < ns; ++q) st[q] = u[slot_comp(kind, q)];
+  }
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(kAsm)
 k_stored_weights(int transform, double tbx, double tby, double tbz, int nmeas,
@@ -643,38 +683,96 @@ k_stored_weights(int transform, double tbx, double tby, double tbz, int nmeas,
   __syncthreads();
   if (t < count) {
     double w[10];
-    if (transform == TR_NONE) {
-#pragma unroll
-      for (int c = 0; c < raw; ++c) w[c] = raw_rec[t * raw + c];
-    } else {
-      const double m = mis[s];
-      const double *d = rawd + n * (long long)nmeas * raw + (long long)s * raw;
-      if (transform == TR_FTG_INVARIANT) {
-        w[0] = mul(m, add(d[4], d[8])); w[1] = mul(m, -d[3]); w[2] = mul(m, -d[6]);
-        w[3] = mul(m, -d[1]); w[4] = mul(m, add(d[0], d[8])); w[5] = mul(m, -d[7]);
-        w[6] = mul(m, -d[2]); w[7] = mul(m, -d[5]); w[8] = mul(m, add(d[0], d[4]));
-      } else if (transform == TR_TOTAL_FIELD) {
-        const double tt = sqrt(add(add(mul(d[0], d[0]), mul(d[1], d[1])), mul(d[2], d[2])));
-        for (int c = 0; c < 3; ++c) w[c] = mul(m, d[c] / tt);
-      } else {
-        w[0] = mul(m, tbx); w[1] = mul(m, tby); w[2] = mul(m, tbz);
-      }
-    }
+    const bool plain = transform == TR_NONE;
+    station_weights<raw>(transform, tbx, tby, tbz, raw_rec + t * raw, plain ? 0.0 : mis[s],
+                         plain ? nullptr : rawd + n * (long long)nmeas * raw + (long long)s * raw,
+                         w);
 #pragma unroll
     for (int c = 0; c < raw; ++c) raw_rec[t * raw + c] = w[c];
-    if constexpr (stored_is_raw(kind)) {
-#pragma unroll
-      for (int c = 0; c < raw; ++c) st_rec[t * ns + c] = w[c];
-    } else {
-      double u[NC_COUNT];
-      comps_from_raw_weights(kind, w, mf, u);
-#pragma unroll
-      for (int q = 0; q < ns; ++q) st_rec[t * ns + q] = u[slot_comp(kind, q)];
-    }
+    stored_weights<kind>(w, mf, st_rec + t * ns);
   }
   __syncthreads();
   copy_records<raw>(w_raw + n * (long long)nmeas * raw + (long long)s0 * raw, raw_rec, count);
   copy_records<ns>(w_st + n * ld_w + (long long)s0 * ns, st_rec, count);
+}
+
+// The stored-row weights of one model and their fp16 split in one launch, for
+// surveys of at most kWsThreads * kWsPer stations: block n computes every
+// station's weights in registers (k_stored_weights' arithmetic, raw-row
+// weights written to w_raw), scales them by J's row scales, takes the row's
+// maximum and splits them (k_split_rows_small's arithmetic) -- the same
+// values as the two launches, without the weights' round trip through HBM.
+// Rows n >= nmod are zero padding (scale 1), as in the split.
+constexpr int kWsThreads = 512;
+constexpr int kWsPer = 2;
+template <int KIND>
+__global__ void __launch_bounds__(kWsThreads)
+k_weights_split(int transform, double tbx, double tby, double tbz, int nmeas, int nmod,
+                const double *__restrict__ misfit, long long ld_misfit,
+                const double *__restrict__ rawd, MagField mf, double *__restrict__ w_raw,
+                const float *__restrict__ colscale, float *__restrict__ rowscale,
+                __half *__restrict__ hi, __half *__restrict__ lo, long long ld_dst) {
+  constexpr int kind = KIND;
+  constexpr int raw = kind_raw(kind);
+  constexpr int ns = stored_rows(kind);
+  const int n = blockIdx.x;
+  double v[kWsPer][ns];
+  float mf32 = 0.0f;
+#pragma unroll
+  for (int k = 0; k < kWsPer; ++k) {
+    const int s = threadIdx.x + k * kWsThreads;
+    if (n < nmod && s < nmeas) {
+      const double *mis = misfit + n * ld_misfit;
+      const bool plain = transform == TR_NONE;
+      double w[10];
+      station_weights<raw>(transform, tbx, tby, tbz, mis + (long long)s * raw,
+                           plain ? 0.0 : mis[s],
+                           plain ? nullptr : rawd + (long long)n * nmeas * raw + (long long)s * raw,
+                           w);
+      double *wr = w_raw + (long long)n * nmeas * raw + (long long)s * raw;
+#pragma unroll
+      for (int c = 0; c < raw; ++c) wr[c] = w[c];
+      stored_weights<kind>(w, mf, v[k]);
+#pragma unroll
+      for (int q = 0; q < ns; ++q) {
+        v[k][q] = v[k][q] * (double)colscale[(long long)s * ns + q];
+        mf32 = fmaxf(mf32, fabsf(approx_f32(v[k][q])));
+      }
+    }
+  }
+  __shared__ double red[kWsThreads / 32];
+  __shared__ float sh_scale;
+  const double m = warp_max_d((double)mf32);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double mm = 0.0;
+    for (int w = 0; w < kWsThreads / 32; ++w) mm = fmax(mm, red[w]);
+    sh_scale = (float)pow2_scale(mm);
+    rowscale[n] = sh_scale;
+  }
+  __syncthreads();
+  const double inv = 1.0 / (double)sh_scale;  // a power of two: exact
+  __half *h = hi + (long long)n * ld_dst;
+  __half *l = lo + (long long)n * ld_dst;
+#pragma unroll
+  for (int k = 0; k < kWsPer; ++k) {
+    const int s = threadIdx.x + k * kWsThreads;
+    if (s < nmeas) {
+#pragma unroll
+      for (int q = 0; q < ns; ++q) {
+        const float x = n < nmod ? f64_to_f32_ftz(fma(v[k][q], inv, 0.0)) : 0.0f;
+        const __half hv = __float2half_rn(x);
+        h[(long long)s * ns + q] = hv;
+        l[(long long)s * ns + q] = __float2half_rn(__fsub_rn(x, __half2float(hv)));
+      }
+    }
+  }
+  // padding columns
+  for (long long c = (long long)nmeas * ns + threadIdx.x; c < ld_dst; c += kWsThreads) {
+    h[c] = __float2half_rn(0.0f);
+    l[c] = __float2half_rn(0.0f);
+  }
 }
 
 // grads[n][ngrid + j] = 2 sum_s sum_r w_raw[n][s][r] bgsens[s][r][j]; block (j, n)
@@ -853,6 +951,34 @@ cudaError_t launch_stored_weights(int kind, int transform, double tbx, double tb
     default: return cudaErrorInvalidValue;
   }
 #undef J3G_WEIGHTS
+  return cudaGetLastError();
+}
+
+bool weights_split_fits(int nmeas, long long ld_dst, int nrow_pad) {
+  return nmeas <= kWsThreads * kWsPer && ld_dst <= kSmallRow && nrow_pad >= 1;
+}
+
+cudaError_t launch_weights_split(int kind, int transform, double tbx, double tby, double tbz,
+                                 int nmeas, int nmod, int nrow_pad, const double *misfit,
+                                 long long ld_misfit, const double *rawd, const MagField &mf,
+                                 double *w_raw, const float *colscale, float *rowscale, void *hi,
+                                 void *lo, long long ld_dst, cudaStream_t st) {
+  if (!weights_split_fits(nmeas, ld_dst, nrow_pad)) return cudaErrorInvalidValue;
+  if ((long long)nmeas * stored_rows(kind) > ld_dst) return cudaErrorInvalidValue;
+#define J3G_WS(K)                                                                             \
+  k_weights_split<K><<<nrow_pad, kWsThreads, 0, st>>>(                                        \
+      transform, tbx, tby, tbz, nmeas, nmod, misfit, ld_misfit, rawd, mf, w_raw, colscale,     \
+      rowscale, static_cast<__half *>(hi), static_cast<__half *>(lo), ld_dst)
+  switch (kind) {
+    case KIND_SCALAR: J3G_WS(KIND_SCALAR); break;
+    case KIND_TENSOR: J3G_WS(KIND_TENSOR); break;
+    case KIND_MAGNETIC: J3G_WS(KIND_MAGNETIC); break;
+    case KIND_JOINT: J3G_WS(KIND_JOINT); break;
+    case KIND_MAG_GRADIENT: J3G_WS(KIND_MAG_GRADIENT); break;
+    case KIND_MAGNETIZATION: J3G_WS(KIND_MAGNETIZATION); break;
+    default: return cudaErrorInvalidValue;
+  }
+#undef J3G_WS
   return cudaGetLastError();
 }
 

@@ -71,6 +71,16 @@ cudaError_t launch_stored_weights(int kind, int transform, double tbx, double tb
                                   int nmeas, int nmod, const double *misfit, long long ld_misfit,
                                   const double *rawd, const MagField &mf, double *w_raw,
                                   double *w_st, long long ld_w, cudaStream_t st);
+// The weights of launch_stored_weights and their split (launch_split_matrix
+// without centring, colscale = J's row scales) in one launch, for surveys
+// that fit one block per model (weights_split_fits): w_raw as
+// launch_stored_weights writes it, hi / lo / rowscale as the split does.
+bool weights_split_fits(int nmeas, long long ld_dst, int nrow_pad);
+cudaError_t launch_weights_split(int kind, int transform, double tbx, double tby, double tbz,
+                                 int nmeas, int nmod, int nrow_pad, const double *misfit,
+                                 long long ld_misfit, const double *rawd, const MagField &mf,
+                                 double *w_raw, const float *colscale, float *rowscale, void *hi,
+                                 void *lo, long long ld_dst, cudaStream_t st);
 cudaError_t launch_bg_grad_batched(int raw, int nmeas, int nbg, int nmod, const double *w_raw,
                                    const double *bgsens, double *grads, long long ld_grads,
                                    long long ngrid, cudaStream_t st);
