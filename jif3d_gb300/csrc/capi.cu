@@ -71,7 +71,7 @@ struct j3g_context {
   long long st_ld = 0;         // cells padded to a multiple of 64
   long long st_ldT = 0;        // rows padded to a multiple of 64 (transposed copy)
   DevBuf J32, Jhi, Jlo, JThi, JTlo, rowscale, Jrowsum;
-  DevBuf x32, sums, part, Bhi, Blo, P, wst, wrawb, rawb, gerr, mscale, mmean, swork;
+  DevBuf x32, sums, part, Bhi, Blo, P, wst, wrawb, rawb, gerr, mscale, mmean, swork, sexp;
 
   // tensor-core product plans (j3g_set_autotune): key direction, rows, padded
   // models, K; the plan last used per direction is kept for j3g_get_gemm_plan
@@ -734,17 +734,49 @@ int choose_splits(long long m, int ntiles, long long ld) {
   return (int)std::max<long long>(1, std::min(s, kb));
 }
 
+// The split-sum kernel's arguments for one product (launch_splitk_reduce).
+struct SplitSums {
+  double *out = nullptr;
+  long long ld_out = 0;
+  const float *rowscale = nullptr, *modscale = nullptr;
+  const int *sexp = nullptr;  // per-split model scales (forward), [models][splits]
+  const double *modmean = nullptr, *rowsum = nullptr;
+  double factor = 1.0;
+};
+
+// One tensor-core product and its split sums, timed as the direction's
+// product and the split sums.
+cudaError_t product_launches(j3g_context *c, int dir, const GemmOperands &g, int nsplit, int tile,
+                             long long ldp, long long slice, const SplitSums &ss) {
+  cudaError_t e;
+  {
+    TimedScope ts(c, dir ? J3G_TIMER_GEMM_ADJOINT : J3G_TIMER_GEMM_FORWARD);
+    e = launch_gemm_x3(g, nsplit, ptr<float>(c->P), ldp, slice, ptr<int>(c->gerr), c->stream,
+                       tile);
+  }
+  if (e != cudaSuccess) return e;
+  ++c->launches;
+  TimedScope ts(c, J3G_TIMER_REDUCE);
+  e = launch_splitk_reduce(ptr<float>(c->P), gemm_splits_used(g.ld, nsplit), slice, (int)g.n,
+                           (int)g.m, ldp, ss.rowscale, ss.modscale, ss.sexp, ss.modmean,
+                           ss.rowsum, ss.factor, ss.out, ss.ld_out, c->stream);
+  if (e == cudaSuccess) ++c->launches;
+  return e;
+}
+
 // Plan of one tensor-core product (K splits and N tile), with the partial-sum
 // buffer c->P sized for it.  Without autotuning, the fixed rule: choose_splits
 // and gemm_n_tile.  With autotuning, the first product of a shape times each
 // candidate -- the fixed plan, split counts that fill the last wave of CTAs on
 // the SMs, and one-SM 128-wide tiles where the pair kernel would run -- once
 // after an untimed run (CUDA events on the context's stream), keeps the
-// fastest for the context's lifetime and reuses it.  Every candidate keeps at
-// most 64 k-blocks per split, the bound that holds the FP32 register sums to
-// their accuracy.
-int gemm_plan(j3g_context *c, int dir, const GemmOperands &g, long long ldp, long long slice,
-              j3g_context::GemmPlan &plan) {
+// fastest for the context's lifetime and reuses it.  A candidate is timed
+// as `run` queues it (nsplit, tile): the product with its split sums, and for
+// the forward the models' split, which follows the product's K splits.
+// Every candidate keeps at most 64 k-blocks per split, the bound that holds
+// the FP32 register sums to their accuracy.
+int gemm_plan(j3g_context *c, int dir, const GemmOperands &g, long long slice,
+              const std::function<cudaError_t(int, int)> &run, j3g_context::GemmPlan &plan) {
   const int tile0 = gemm_n_tile((int)g.n);
   plan.tile = tile0;
   plan.nsplit = choose_splits(g.m, (int)(g.n_pad / tile0), g.ld);
@@ -795,25 +827,24 @@ int gemm_plan(j3g_context *c, int dir, const GemmOperands &g, long long ldp, lon
   for (auto &p : cand) nsp_max = std::max(nsp_max, gemm_splits_used(g.ld, p.second));
 
   J3G_TRY(ensure(c, c->P, sizeof(float) * (size_t)nsp_max * slice));
-  float *P = ptr<float>(c->P);
   GemmOperands gt = g;
   gt.fault = 0;  // candidates are timed on the normal path
   cudaEvent_t a, b;
   J3G_CUDA(c, cudaEventCreate(&a));
   J3G_CUDA(c, cudaEventCreate(&b));
+  const bool timing = c->timing;
+  c->timing = false;  // the candidates stay out of the phase timers
   float best = 0.0f;
   for (auto &p : cand) {
     float ms = 0.0f;
-    cudaError_t e = launch_gemm_x3(gt, p.second, P, ldp, slice, ptr<int>(c->gerr), c->stream,
-                                   p.first);
+    cudaError_t e = run(p.second, p.first);
     if (e == cudaSuccess) e = cudaEventRecord(a, c->stream);
-    if (e == cudaSuccess)
-      e = launch_gemm_x3(gt, p.second, P, ldp, slice, ptr<int>(c->gerr), c->stream, p.first);
+    if (e == cudaSuccess) e = run(p.second, p.first);
     if (e == cudaSuccess) e = cudaEventRecord(b, c->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(b);
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
-    c->launches += 2;
     if (e != cudaSuccess) {
+      c->timing = timing;
       cudaEventDestroy(a);
       cudaEventDestroy(b);
       return cuda_fail(c, e, "gemm autotune");
@@ -825,6 +856,7 @@ int gemm_plan(j3g_context *c, int dir, const GemmOperands &g, long long ldp, lon
       plan.ms = ms;
     }
   }
+  c->timing = timing;
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   c->plans[key] = plan;
@@ -856,37 +888,44 @@ int batched_forward_pass(j3g_context *c, int nmod, const double *d_models, doubl
     const long long npad = (nmod + tile - 1) / tile * tile;
     J3G_TRY(ensure(c, c->Bhi, 2 * (size_t)npad * ldK));
     J3G_TRY(ensure(c, c->Blo, 2 * (size_t)npad * ldK));
-    J3G_TRY(ensure(c, c->mscale, sizeof(float) * (size_t)npad));
     J3G_TRY(ensure(c, c->mmean, sizeof(double) * (size_t)npad));
-    J3G_TRY(ensure(c, c->swork, sizeof(double) * (size_t)split_matrix_work((int)npad, ldK)));
-    // models are centred (m - mean over cells); mean * (J 1) is added back in
-    // FP64 after the product, so a large uniform part of a model -- whose
-    // tensor response is nearly zero -- does not eat into the FP32 accuracy
-    {
-      TimedScope ts(c, J3G_TIMER_SPLIT);
-      J3G_LAUNCH(c, launch_split_matrix(d_models, np, nmod, K, nullptr, c->Bhi.p, c->Blo.p, ldK,
-                                        (int)npad, ptr<float>(c->mscale), ptr<double>(c->mmean),
-                                        ptr<double>(c->swork), c->stream));
-      c->launches += split_matrix_launches(true, ldK) - 1;
-    }
+    // split exponents [npad][splits] and the sampled row exponents after them
+    J3G_TRY(ensure(c, c->sexp, sizeof(int) * (size_t)npad * (ldK / 64 + 1)));
     const long long slice = (long long)nmod * R;
     GemmOperands g{c->Jhi.p, c->Jlo.p, R, c->Bhi.p, c->Blo.p, nmod, npad, ldK, true};
     g.fault = c->test_fault;
     J3G_TRY(ensure(c, c->gerr, sizeof(int)));
+    // sums = rowscale * (split sums, each split at its models' scale)
+    //        + centre * (J 1)
+    SplitSums ss;
+    ss.out = ptr<double>(c->sums);
+    ss.ld_out = R;
+    ss.rowscale = ptr<float>(c->rowscale);
+    ss.sexp = ptr<int>(c->sexp);
+    ss.modmean = ptr<double>(c->mmean);
+    ss.rowsum = ptr<double>(c->Jrowsum);
+    // models are centred (m - an estimate of their mean over cells; centre *
+    // (J 1) is added back in FP64 after the product, so a large uniform part
+    // of a model -- whose tensor response is nearly zero -- does not eat into
+    // the FP32 accuracy) and split with one scale per K split of the product
+    auto run = [&](int nsplit, int tile) -> cudaError_t {
+      const int nsp = gemm_splits_used(ldK, nsplit);
+      cudaError_t e;
+      {
+        TimedScope ts(c, J3G_TIMER_SPLIT);
+        e = launch_split_models(d_models, np, nmod, K, c->Bhi.p, c->Blo.p, ldK, (int)npad,
+                                64LL * gemm_kb_per_split(ldK, nsplit), nsp,
+                                ptr<double>(c->mmean), ptr<int>(c->sexp), c->stream);
+      }
+      if (e != cudaSuccess) return e;
+      c->launches += 2;
+      return product_launches(c, 0, g, nsplit, tile, R, slice, ss);
+    };
     j3g_context::GemmPlan plan;
-    J3G_TRY(gemm_plan(c, 0, g, R, slice, plan));
+    J3G_TRY(gemm_plan(c, 0, g, slice, run, plan));
     c->last_plan[0] = plan;
-    const int nsp = gemm_splits_used(ldK, plan.nsplit);
-    {
-      TimedScope ts(c, J3G_TIMER_GEMM_FORWARD);
-      J3G_LAUNCH(c, launch_gemm_x3(g, plan.nsplit, ptr<float>(c->P), R, slice,
-                                   ptr<int>(c->gerr), c->stream, plan.tile));
-    }
-    TimedScope ts(c, J3G_TIMER_REDUCE);
-    J3G_LAUNCH(c, launch_splitk_reduce(ptr<float>(c->P), nsp, slice, nmod, (int)R, R,
-                                       ptr<float>(c->rowscale), ptr<float>(c->mscale),
-                                       ptr<double>(c->mmean), ptr<double>(c->Jrowsum), 1.0,
-                                       ptr<double>(c->sums), R, c->stream));
+    const cudaError_t e = run(plan.nsplit, plan.tile);
+    if (e != cudaSuccess) return cuda_fail(c, e, "forward product");
   }
   TimedScope ts(c, J3G_TIMER_EPILOGUE);
   J3G_LAUNCH(c, launch_stored_assemble(c->kind, c->transform, tbx, tby, tbz, c->nmeas, nmod,
@@ -959,26 +998,26 @@ int batched_adjoint_pass(j3g_context *c, int nmod, const double *d_models,
       TimedScope ts(c, J3G_TIMER_SPLIT);
       J3G_LAUNCH(c, launch_split_matrix(ptr<double>(c->wst), R, nmod, R, ptr<float>(c->rowscale),
                                         c->Bhi.p, c->Blo.p, ldR, (int)npad, ptr<float>(c->mscale),
-                                        nullptr, ptr<double>(c->swork), c->stream));
-      c->launches += split_matrix_launches(false, ldR) - 1;
+                                        ptr<double>(c->swork), c->stream));
+      c->launches += split_matrix_launches(ldR) - 1;
     }
     const long long slice = (long long)nmod * K;
     GemmOperands g{c->JThi.p, c->JTlo.p, K, c->Bhi.p, c->Blo.p, nmod, npad, ldR, true};
     g.fault = c->test_fault;
     J3G_TRY(ensure(c, c->gerr, sizeof(int)));
+    SplitSums ss;  // gradients = 2 * modscale * (split sums)
+    ss.out = d_grads;
+    ss.ld_out = np;
+    ss.modscale = ptr<float>(c->mscale);
+    ss.factor = 2.0;
+    auto run = [&](int nsplit, int tile) {
+      return product_launches(c, 1, g, nsplit, tile, K, slice, ss);
+    };
     j3g_context::GemmPlan plan;
-    J3G_TRY(gemm_plan(c, 1, g, K, slice, plan));
+    J3G_TRY(gemm_plan(c, 1, g, slice, run, plan));
     c->last_plan[1] = plan;
-    const int nsp = gemm_splits_used(ldR, plan.nsplit);
-    {
-      TimedScope ts(c, J3G_TIMER_GEMM_ADJOINT);
-      J3G_LAUNCH(c, launch_gemm_x3(g, plan.nsplit, ptr<float>(c->P), K, slice,
-                                   ptr<int>(c->gerr), c->stream, plan.tile));
-    }
-    TimedScope ts(c, J3G_TIMER_REDUCE);
-    J3G_LAUNCH(c, launch_splitk_reduce(ptr<float>(c->P), nsp, slice, nmod, (int)K, K, nullptr,
-                                       ptr<float>(c->mscale), nullptr, nullptr, 2.0, d_grads, np,
-                                       c->stream));
+    const cudaError_t e = product_launches(c, 1, g, plan.nsplit, plan.tile, K, slice, ss);
+    if (e != cudaSuccess) return cuda_fail(c, e, "adjoint product");
   }
   if (nbg) {
     TimedScope ts(c, J3G_TIMER_EPILOGUE);
@@ -1065,7 +1104,7 @@ int j3g_destroy(j3g_context *c) {
                     &c->G, &c->F, &c->rows, &c->rowsum, &c->probe, &c->J32, &c->Jhi,
                     &c->Jlo, &c->JThi, &c->JTlo, &c->rowscale, &c->x32, &c->sums, &c->part,
                     &c->Bhi, &c->Blo, &c->P, &c->wst, &c->wrawb, &c->rawb, &c->gerr,
-                    &c->mscale, &c->Jrowsum, &c->mmean, &c->swork, &c->chunks, &c->rmaps,
+                    &c->mscale, &c->Jrowsum, &c->mmean, &c->swork, &c->sexp, &c->chunks, &c->rmaps,
                     &c->rcoarse, &c->rfine};
   for (DevBuf *b : bufs)
     if (b->p) cudaFree(b->p);

@@ -63,6 +63,14 @@ __device__ __forceinline__ double f32_to_f64(float f) {
       (long long)(s | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29)));
 }
 
+// d * 2^k by FP64 multiplies: the rare cases of scale_pow2, out of line so
+// that the compiler cannot evaluate them for every element (a select of both
+// arms would put FP64 work on every element, and the FP64 pipe retires about
+// two operations per clock per SM).
+static __device__ __noinline__ double scale_pow2_mul(double d, int k) {
+  return d * ldexp(1.0, k);
+}
+
 // d * 2^k for a normal d whose result stays normal, by an exponent add;
 // zeros pass through; other cases (subnormal, out of range) multiply.
 __device__ __forceinline__ double scale_pow2(double d, int k) {
@@ -71,7 +79,18 @@ __device__ __forceinline__ double scale_pow2(double d, int k) {
   const int e = (int)((b >> 52) & 0x7ff);
   if (e > 0 && e < 0x7ff && e + k > 0 && e + k < 0x7ff)
     return __longlong_as_double(b + ((long long)k << 52));
-  return d * ldexp(1.0, k);
+  return scale_pow2_mul(d, k);
+}
+
+// f * 2^k by an exponent add, branch-free: exact while the result stays a
+// normal float; results below the normal range and subnormal f become a
+// signed zero, results above it a signed infinity; infinities and NaNs pass
+// through.
+__device__ __forceinline__ float scale_f32_ftz(float f, int k) {
+  const uint32_t u = __float_as_uint(f), s = u & 0x80000000u;
+  const int e = (int)((u >> 23) & 0xffu), ek = e + k;
+  const uint32_t scaled = ek <= 0 ? s : (ek >= 0xff ? (s | 0x7f800000u) : u + ((uint32_t)k << 23));
+  return __uint_as_float(e == 0xff ? u : (e == 0 ? s : scaled));
 }
 
 // Exponent k of a power-of-two float 2^k (normal range).

@@ -831,6 +831,11 @@ cudaError_t launch_pair(const GemmOperands &g, int nsplit, float *P, long long l
 // N tile of the batched products: 64 or 128 on one SM, 256 on a CTA pair.
 int gemm_n_tile(int n) { return n <= 64 ? 64 : (n <= 128 ? 128 : kPairN); }
 
+int gemm_kb_per_split(long long ld, int nsplit) {
+  const int kb_total = (int)(ld / BK);
+  return (kb_total + nsplit - 1) / nsplit;
+}
+
 int gemm_splits_used(long long ld, int nsplit) {
   const int kb_total = (int)(ld / BK);
   const int kb_per = (kb_total + nsplit - 1) / nsplit;

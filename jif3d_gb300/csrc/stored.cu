@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 
@@ -142,13 +143,13 @@ __global__ void k_transpose16(const uint16_t *__restrict__ in, long long ld_in, 
   }
 }
 
-// Splitting an FP64 matrix [nrow][ld_src] (rows = models or residual vectors)
-// into fp16 hi / lo rows [nrow_pad][ld_dst], in three grid-wide passes so that
-// a few hundred long rows still fill the GPU:
-//   k_row_stats     per (row, column chunk): max |v| and sum v
-//   k_row_finalize  per row: power-of-two scale, optional mean (centring)
-//   k_split_chunks  per (row, column chunk): (v - mean) / scale -> hi + lo
-// Short rows without centring go in one pass (k_split_rows_small).
+// Splitting an FP64 matrix [nrow][ld_src] (the adjoint's scaled residual
+// rows) into fp16 hi / lo rows [nrow_pad][ld_dst], in three grid-wide passes
+// so that a few hundred long rows still fill the GPU:
+//   k_row_stats     per (row, column chunk): max |v|
+//   k_row_finalize  per row: power-of-two scale
+//   k_split_chunks  per (row, column chunk): v / scale -> hi + lo
+// Short rows go in one pass (k_split_rows_small).
 // v = src[r][c] * colscale[c] (colscale optional).
 constexpr int kChunk = 8192;
 constexpr long long kSmallRow = 16384;  // rows up to this length split in one pass
@@ -172,29 +173,22 @@ __device__ __forceinline__ double scaled_val(const double *src, long long ld_src
 
 __global__ void k_row_stats(const double *__restrict__ src, long long ld_src, int nrow,
                             long long ncol, const float *__restrict__ colscale,
-                            double *__restrict__ part_max, double *__restrict__ part_sum,
-                            int nchunk, int chunk) {
+                            double *__restrict__ part_max, int nchunk, int chunk) {
   const long long r = blockIdx.y;
   const long long c0 = (long long)blockIdx.x * chunk + threadIdx.x;
-  // The scale needs only the binade of max |v| (truncating the mantissa keeps
-  // it) and the centring mean only an estimate (the same value is added back
-  // after the product), so both run in FP32 on truncated values.
-  float mf = 0.0f, sf = 0.0f;
+  // the scale needs only the binade of max |v|: truncating the mantissa keeps
+  // it, so the maximum runs in FP32 on truncated values
+  float mf = 0.0f;
   for (int j0 = 0; j0 < chunk / kT; j0 += kBatch) {
     double v[kBatch];  // a batch of independent loads in flight per thread
 #pragma unroll
     for (int u = 0; u < kBatch; ++u)
       v[u] = scaled_val(src, ld_src, nrow, ncol, colscale, r, c0 + (long long)(j0 + u) * kT);
 #pragma unroll
-    for (int u = 0; u < kBatch; ++u) {
-      const float a = approx_f32(v[u]);
-      mf = fmaxf(mf, fabsf(a));
-      sf += a;
-    }
+    for (int u = 0; u < kBatch; ++u) mf = fmaxf(mf, fabsf(approx_f32(v[u])));
   }
-  double m = (double)mf, sum = (double)sf;
   __shared__ double red[kT / 32];
-  m = warp_max_d(m);
+  const double m = warp_max_d((double)mf);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -202,37 +196,24 @@ __global__ void k_row_stats(const double *__restrict__ src, long long ld_src, in
     for (int w = 0; w < kT / 32; ++w) mm = fmax(mm, red[w]);
     part_max[r * nchunk + blockIdx.x] = mm;
   }
-  __syncthreads();
-  sum = block_sum_d<kT>(sum, red);
-  if (threadIdx.x == 0) part_sum[r * nchunk + blockIdx.x] = sum;
 }
 
-__global__ void k_row_finalize(int nrow_pad, int nchunk, long long ncol, bool center,
-                               const double *__restrict__ part_max,
-                               const double *__restrict__ part_sum, float *__restrict__ rowscale,
-                               double *__restrict__ rowmean) {
+__global__ void k_row_finalize(int nrow_pad, int nchunk, const double *__restrict__ part_max,
+                               float *__restrict__ rowscale) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrow_pad) return;
-  double mx = 0.0, sum = 0.0;
-  for (int k = 0; k < nchunk; ++k) {
-    mx = fmax(mx, part_max[(long long)r * nchunk + k]);
-    sum += part_sum[(long long)r * nchunk + k];
-  }
-  const double mean = (center && ncol > 0) ? sum / (double)ncol : 0.0;
-  // |v - mean| <= max|v| + |mean| <= 2 max|v|
-  rowscale[r] = (float)pow2_scale(center ? 2.0 * mx : mx);
-  if (rowmean) rowmean[r] = mean;
+  double mx = 0.0;
+  for (int k = 0; k < nchunk; ++k) mx = fmax(mx, part_max[(long long)r * nchunk + k]);
+  rowscale[r] = (float)pow2_scale(mx);
 }
 
 __global__ void k_split_chunks(const double *__restrict__ src, long long ld_src, int nrow,
                                long long ncol, const float *__restrict__ colscale,
-                               const float *__restrict__ rowscale,
-                               const double *__restrict__ rowmean, __half *__restrict__ hi,
+                               const float *__restrict__ rowscale, __half *__restrict__ hi,
                                __half *__restrict__ lo, long long ld_dst, int chunk) {
   const long long r = blockIdx.y;
   const long long c0 = (long long)blockIdx.x * chunk + threadIdx.x;
   const double inv = 1.0 / (double)rowscale[r];  // a power of two: exact
-  const double shift = rowmean ? -rowmean[r] * inv : 0.0;
   for (int j0 = 0; j0 < chunk / kT; j0 += kBatch) {
     double v[kBatch];
 #pragma unroll
@@ -242,12 +223,164 @@ __global__ void k_split_chunks(const double *__restrict__ src, long long ld_src,
     for (int u = 0; u < kBatch; ++u) {
       const long long c = c0 + (long long)(j0 + u) * kT;
       if (c >= ld_dst) break;
-      // one FP64 operation per element, (v - mean) / scale; then FP32: the
-      // 24-bit float keeps more than the 22 bits that hi + lo carry
-      const float x = (r < nrow && c < ncol) ? f64_to_f32_ftz(fma(v[u], inv, shift)) : 0.0f;
+      // v / scale (exact), then FP32: the 24-bit float keeps more than the
+      // 22 bits that hi + lo carry
+      const float x = (r < nrow && c < ncol) ? f64_to_f32_ftz(v[u] * inv) : 0.0f;
       const __half hv = __float2half_rn(x);
       hi[r * ld_dst + c] = hv;
       lo[r * ld_dst + c] = __float2half_rn(__fsub_rn(x, __half2float(hv)));
+    }
+  }
+}
+
+// Models for the forward product, split in one pass over HBM (the three
+// passes above read every model twice).  Any centre is exact -- c * (J 1) is
+// added back after the product; it only has to take out the bulk of a large
+// uniform part -- so each row's centre is an estimate from a sample of its
+// values.  The power-of-two scale only sets the fp16 exponent range (hi and
+// lo keep 11 bits each at any scale that keeps them normal), so a row scale
+// taken from the same sample serves every K split of the product whose
+// values it bounds; a split with larger values takes its own, larger scale,
+// known before its split because one block holds the split's columns.  The
+// split-sum kernel applies each split's scale (sexp) to its partial sums.
+constexpr int kCentreRuns = 64;    // contiguous runs sampled per model row
+constexpr int kCentreRun = 32;     // values per run
+constexpr int kScaleMargin = 2;    // binades of headroom on the sampled scale
+__global__ void __launch_bounds__(kT) k_model_centre(const double *__restrict__ src,
+                                                     long long ld_src, int nrow, long long ncol,
+                                                     double *__restrict__ centre,
+                                                     int *__restrict__ eref) {
+  constexpr int kPer = kCentreRuns * kCentreRun / kT;
+  const int r = blockIdx.x;
+  // run j starts at j * ncol / kCentreRuns (runs overlap when ncol is small)
+  double v[kPer];
+  int cnt = 0;
+#pragma unroll
+  for (int u = 0; u < kPer; ++u) {
+    const int i = threadIdx.x + u * kT, j = i / kCentreRun;
+    const long long c = (long long)j * ncol / kCentreRuns + i % kCentreRun;
+    const bool ok = r < nrow && c < ncol;
+    v[u] = ok ? src[(long long)r * ld_src + c] : 0.0;
+    cnt += ok;
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int u = 0; u < kPer; ++u) s += v[u];
+  __shared__ double red[kT / 32];
+  __shared__ double sh_c;
+  s = block_sum_d<kT>(s, red);
+  const double n = block_sum_d<kT>((double)cnt, red);
+  if (threadIdx.x == 0) sh_c = n > 0.0 ? s / n : 0.0;
+  __syncthreads();
+  const float c32 = approx_f32(sh_c);
+  float mf = 0.0f;
+#pragma unroll
+  for (int u = 0; u < kPer; ++u) mf = fmaxf(mf, fabsf(approx_f32(v[u]) - c32));
+  const double m = warp_max_d((double)mf);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double mm = 0.0;
+    for (int w = 0; w < kT / 32; ++w) mm = fmax(mm, red[w]);
+    centre[r] = sh_c;
+    // frexp exponent of the sampled maximum, minus 14, plus the margin; an
+    // all-equal sample leaves it to the splits' own maxima
+    int e = 0;
+    if (mm > 0.0) frexp(mm, &e);
+    eref[r] = mm > 0.0 ? e - 14 + kScaleMargin : INT_MIN / 2;
+  }
+}
+
+// One block per (model row, K split): d = v - centre (the one FP64 operation
+// per element), rounded to float and kept in registers; the split's exponent
+// e = max(eref[row], frexp exponent of max |d| - 14) (sexp[row][split]), so
+// |d| / 2^e < 2^14; then hi + lo of d / 2^e (a float multiply by a power of
+// two: exact, one rounding in all, for the exponents of any physical model;
+// others take the FP64 scaling).  Splits of up to kT * kSplitPer columns
+// keep the values in registers; wider ones (plans pinned past the accuracy
+// bound, WIDE) compute them again in the second pass.
+constexpr int kSplitPer = 16;
+template <bool WIDE>
+__global__ void __launch_bounds__(kT) k_split_models(
+    const double *__restrict__ src, long long ld_src, int nrow, long long ncol,
+    const double *__restrict__ centre, const int *__restrict__ eref, __half *__restrict__ hi,
+    __half *__restrict__ lo, long long ld_dst, long long cols_per_split, int nsp,
+    int *__restrict__ sexp) {
+  const long long r = blockIdx.y;
+  const long long c0 = (long long)blockIdx.x * cols_per_split;
+  const long long c1 = min(ld_dst, c0 + cols_per_split);
+  const bool row_ok = r < nrow;
+  const double cr = row_ok ? centre[r] : 0.0;
+  const double *row = src + r * ld_src;
+  constexpr bool in_regs = !WIDE;
+  float x[kSplitPer];
+  float mf = 0.0f;
+  if constexpr (in_regs) {
+    double v[kSplitPer];
+#pragma unroll
+    for (int u = 0; u < kSplitPer; ++u) {
+      const long long c = c0 + threadIdx.x + (long long)u * kT;
+      v[u] = (row_ok && c < c1 && c < ncol) ? row[c] : cr;
+    }
+#pragma unroll
+    for (int u = 0; u < kSplitPer; ++u) {
+      x[u] = f64_to_f32_ftz(v[u] - cr);
+      mf = fmaxf(mf, fabsf(x[u]));
+    }
+  } else {
+    for (long long c = c0 + threadIdx.x; c < c1; c += kT)
+      if (row_ok && c < ncol) mf = fmaxf(mf, fabsf(f64_to_f32_ftz(row[c] - cr)));
+  }
+  __shared__ float red[kT / 32];
+  __shared__ int sh_e;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mf = fmaxf(mf, __shfl_down_sync(0xffffffffu, mf, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mf;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = 0.0f;
+    for (int w = 0; w < kT / 32; ++w) m = fmaxf(m, red[w]);
+    // m in [2^(E-1), 2^E) with E = biased exponent - 126; rounding to float
+    // can lift a maximum just below 2^E to 2^E, which only raises E
+    const uint32_t be = (__float_as_uint(m) >> 23) & 0xffu;
+    const int el = be ? (int)be - 126 - 14 : INT_MIN / 2;
+    int e = max(row_ok ? eref[r] : 0, el);
+    if (e == INT_MIN / 2) e = 0;  // all zero
+    sh_e = e;
+    sexp[r * nsp + blockIdx.x] = e;
+  }
+  __syncthreads();
+  const int e = sh_e;
+  const bool fast = e >= -100 && e <= 100;  // float scaling exact, no overflow
+  const float inv = fast ? __uint_as_float((uint32_t)(127 - e) << 23) : 0.0f;
+  // 2^-e as a double (the split exponents of finite doubles stay within
+  // -1100 .. 1040; beyond the normal range the scaling saturates)
+  const int eb = min(2046, max(1, 1023 - e));
+  const double inv64 = __longlong_as_double((long long)eb << 52);
+  auto put = [&](long long c, float xf, double dv) {
+    const float xs = fast ? xf * inv : f64_to_f32_ftz(dv * inv64);
+    const __half hv = __float2half_rn(xs);
+    hi[r * ld_dst + c] = hv;
+    lo[r * ld_dst + c] = __float2half_rn(__fsub_rn(xs, __half2float(hv)));
+  };
+  if constexpr (in_regs) {
+    if (fast) {
+#pragma unroll
+      for (int u = 0; u < kSplitPer; ++u) {
+        const long long c = c0 + threadIdx.x + (long long)u * kT;
+        if (c < c1) put(c, x[u], 0.0);
+      }
+    } else {
+      for (int u = 0; u < kSplitPer; ++u) {
+        const long long c = c0 + threadIdx.x + (long long)u * kT;
+        if (c < c1) put(c, 0.0f, (row_ok && c < ncol) ? row[c] - cr : 0.0);
+      }
+    }
+  } else {
+    for (long long c = c0 + threadIdx.x; c < c1; c += kT) {
+      const double dv = (row_ok && c < ncol) ? row[c] - cr : 0.0;
+      put(c, f64_to_f32_ftz(dv), dv);
     }
   }
 }
@@ -406,9 +539,11 @@ __global__ void k_sum_parts(const double *__restrict__ part, int nchunk, long lo
 
 // out[n][r] = factor * rowscale[r] * modscale[n] * sum_s P[s][n][r]
 // (FP64 reduction of split-K partials; either scale may be absent)
+// sexp (optional, [nmod][nsplit]): split s of model n carries the scale
+// 2^sexp[n][s] (models split per K split, k_split_models) in place of modscale.
 __global__ void k_splitk_reduce(const float *__restrict__ P, int nsplit, long long slice,
                                 int nmod, int nrow, long long ldp, const float *__restrict__ rowscale,
-                                const float *__restrict__ modscale,
+                                const float *__restrict__ modscale, const int *__restrict__ sexp,
                                 const double *__restrict__ modmean,
                                 const double *__restrict__ rowsum, double factor,
                                 double *__restrict__ out, long long ld_out) {
@@ -416,16 +551,21 @@ __global__ void k_splitk_reduce(const float *__restrict__ P, int nsplit, long lo
   if (t >= (long long)nmod * nrow) return;
   const int n = t / nrow, r = t % nrow;
   const float *p = P + (long long)n * ldp + r;
+  const int *se = sexp ? sexp + (long long)n * nsplit : nullptr;
+  auto part = [&](int s) {
+    const double x = (double)p[(long long)s * slice];
+    return se ? x * ldexp(1.0, se[s]) : x;
+  };
   // independent partial sums keep several loads in flight
   double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
   int s = 0;
   for (; s + 3 < nsplit; s += 4) {
-    v0 += (double)p[(long long)s * slice];
-    v1 += (double)p[(long long)(s + 1) * slice];
-    v2 += (double)p[(long long)(s + 2) * slice];
-    v3 += (double)p[(long long)(s + 3) * slice];
+    v0 += part(s);
+    v1 += part(s + 1);
+    v2 += part(s + 2);
+    v3 += part(s + 3);
   }
-  for (; s < nsplit; ++s) v0 += (double)p[(long long)s * slice];
+  for (; s < nsplit; ++s) v0 += part(s);
   double v = (v0 + v1) + (v2 + v3);
   if (rowscale) v *= (double)rowscale[r];
   if (modscale) v *= (double)modscale[n];
@@ -448,8 +588,8 @@ __global__ void k_splitk_reduce(const float *__restrict__ P, int nsplit, long lo
 // FP32 first (relative 2^-24, below the FP32 rounding each partial already
 // carries) so that the pass stays at HBM speed: one FP64 operation per output
 // costs as much as the whole memory traffic on this GPU's FP64 pipe.  The
-// power-of-two scales are exponent adds; factor is applied the same way when
-// it is a power of two (fpow2, 2^kfac), else by an FP64 multiply.
+// power-of-two scales and the factor (a power of two, 2^kfac; other factors
+// take k_splitk_reduce) are exponent adds.
 constexpr int kPairSplits = 4;
 // G: row quads per thread (2 for a few splits; 1 for many, so that more
 // threads share the splits' loads); U: splits per load batch.  The next
@@ -458,11 +598,21 @@ template <bool PAIR, int G>  // PAIR: widen hi + lo in FP64 (more than kPairSpli
 __global__ void __launch_bounds__(kT) k_splitk_reduce4(
     const float *__restrict__ P, int nsplit, long long slice, int nrow, long long ldp,
     const float *__restrict__ rowscale, const float *__restrict__ modscale,
-    const double *__restrict__ modmean, const double *__restrict__ rowsum, bool fpow2, int kfac,
-    double factor, double *__restrict__ out, long long ld_out) {
+    const int *__restrict__ sexp, const double *__restrict__ modmean,
+    const double *__restrict__ rowsum, int kfac, double *__restrict__ out, long long ld_out) {
   constexpr int U = G == 1 ? 8 : 2;
   const int nq = nrow / 4;
   const int n = blockIdx.y;
+  // per-split scales 2^sexp[n][s]: each split's partials are brought to the
+  // smallest of them in FP32 (exact: an exponent add; most splits of a model
+  // share one scale and skip it) and that one is applied with the other
+  // scales at the end
+  const int *se = sexp ? sexp + (long long)n * nsplit : nullptr;
+  int ebase = 0;
+  if (se) {
+    ebase = se[0];
+    for (int s = 1; s < nsplit; ++s) ebase = min(ebase, se[s]);
+  }
   const int q0 = blockIdx.x * (kT * G) + threadIdx.x;
   const long long s4 = slice / 4;
   const float4 *p = reinterpret_cast<const float4 *>(P + (long long)n * ldp);
@@ -499,7 +649,14 @@ __global__ void __launch_bounds__(kT) k_splitk_reduce4(
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         if (s + u >= nsplit) continue;
-        const float x[4] = {q[g][u].x, q[g][u].y, q[g][u].z, q[g][u].w};
+        float x[4] = {q[g][u].x, q[g][u].y, q[g][u].z, q[g][u].w};
+        if (se) {
+          const int k = se[s + u] - ebase;
+          if (k != 0) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) x[i] = scale_f32_ftz(x[i], k);
+          }
+        }
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           float sres, err;
@@ -524,7 +681,7 @@ __global__ void __launch_bounds__(kT) k_splitk_reduce4(
         }
     }
   }
-  const int kmod = (modscale ? pow2_exponent(modscale[n]) : 0) + (fpow2 ? kfac : 0);
+  const int kmod = (modscale ? pow2_exponent(modscale[n]) : 0) + ebase + kfac;
 #pragma unroll
   for (int g = 0; g < G; ++g) {
     const int qi = q0 + g * kT;
@@ -537,9 +694,8 @@ __global__ void __launch_bounds__(kT) k_splitk_reduce4(
       double v = PAIR ? f32_to_f64(hi[g][i]) + f32_to_f64(lo[g][i])
                       : f32_to_f64(__fadd_rn(hi[g][i], lo[g][i]));
       v = scale_pow2(v, kmod + (rowscale ? pow2_exponent(rowscale[r + i]) : 0));
-      if (modmean)
-        v = fma(modmean[n], fpow2 ? scale_pow2(rowsum[r + i], kfac) : rowsum[r + i], v);
-      res[i] = fpow2 ? v : factor * v;
+      if (modmean) v = fma(modmean[n], scale_pow2(rowsum[r + i], kfac), v);
+      res[i] = v;
     }
     double *o = out + (long long)n * ld_out + r;
     // whole 16-byte stores where the output row allows (full sectors per warp)
@@ -815,40 +971,60 @@ cudaError_t launch_transpose16(const void *in, long long ld_in, long long rows, 
   return cudaGetLastError();
 }
 
-int split_matrix_launches(bool center, long long ld_dst) {
-  return (!center && ld_dst <= kSmallRow) ? 1 : 3;
-}
+int split_matrix_launches(long long ld_dst) { return ld_dst <= kSmallRow ? 1 : 3; }
 
 long long split_matrix_work(int nrow_pad, long long ld_dst) {
   const long long chunk = split_chunk(nrow_pad, ld_dst);
-  return 2LL * nrow_pad * ((ld_dst + chunk - 1) / chunk);
+  return (long long)nrow_pad * ((ld_dst + chunk - 1) / chunk);
 }
 
 cudaError_t launch_split_matrix(const double *src, long long ld_src, int nrow, long long ncol,
                                 const float *colscale, void *hi, void *lo, long long ld_dst,
-                                int nrow_pad, float *rowscale, double *rowmean, double *work,
-                                cudaStream_t st) {
+                                int nrow_pad, float *rowscale, double *work, cudaStream_t st) {
   if (nrow_pad == 0) return cudaSuccess;
   const int chunk = (int)split_chunk(nrow_pad, ld_dst);
   const int nchunk = cdiv(ld_dst, chunk);
-  if (!rowmean && ld_dst <= kSmallRow) {
+  if (ld_dst <= kSmallRow) {
     k_split_rows_small<<<nrow_pad, kSmallT, 0, st>>>(src, ld_src, nrow, ncol, colscale, rowscale,
                                                 static_cast<__half *>(hi),
                                                 static_cast<__half *>(lo), ld_dst);
     return cudaGetLastError();
   }
-  double *pmax = work, *psum = work + (long long)nrow_pad * nchunk;
   dim3 grid(nchunk, nrow_pad);
-  k_row_stats<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, pmax, psum, nchunk, chunk);
+  k_row_stats<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, work, nchunk, chunk);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_row_finalize<<<cdiv(nrow_pad, 128), 128, 0, st>>>(nrow_pad, nchunk, ncol, rowmean != nullptr,
-                                                      pmax, psum, rowscale, rowmean);
+  k_row_finalize<<<cdiv(nrow_pad, 128), 128, 0, st>>>(nrow_pad, nchunk, work, rowscale);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_split_chunks<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, rowscale, rowmean,
+  k_split_chunks<<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, colscale, rowscale,
                                       static_cast<__half *>(hi), static_cast<__half *>(lo),
                                       ld_dst, chunk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_split_models(const double *src, long long ld_src, int nrow, long long ncol,
+                                void *hi, void *lo, long long ld_dst, int nrow_pad,
+                                long long cols_per_split, int nsp, double *centre, int *sexp,
+                                cudaStream_t st) {
+  if (nrow_pad == 0) return cudaSuccess;
+  if (nrow_pad > 65535 || cols_per_split <= 0 || (long long)nsp * cols_per_split < ld_dst)
+    return cudaErrorInvalidValue;
+  int *eref = sexp + (long long)nrow_pad * nsp;  // the sampled row exponents
+  k_model_centre<<<nrow_pad, kT, 0, st>>>(src, ld_src, nrow, ncol, centre, eref);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  dim3 grid(nsp, nrow_pad);
+  if (cols_per_split <= (long long)kT * kSplitPer)
+    k_split_models<false><<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, centre, eref,
+                                               static_cast<__half *>(hi),
+                                               static_cast<__half *>(lo), ld_dst,
+                                               cols_per_split, nsp, sexp);
+  else
+    k_split_models<true><<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, centre, eref,
+                                              static_cast<__half *>(hi),
+                                              static_cast<__half *>(lo), ld_dst, cols_per_split,
+                                              nsp, sexp);
   return cudaGetLastError();
 }
 
@@ -881,29 +1057,30 @@ cudaError_t launch_gemv_t_f32(const float *J, long long ld, int nrows, const dou
 
 cudaError_t launch_splitk_reduce(const float *P, int nsplit, long long slice, int nmod, int nrow,
                                  long long ldp, const float *rowscale, const float *modscale,
-                                 const double *modmean, const double *rowsum, double factor,
-                                 double *out, long long ld_out, cudaStream_t st) {
+                                 const int *sexp, const double *modmean, const double *rowsum,
+                                 double factor, double *out, long long ld_out, cudaStream_t st) {
   const long long n = (long long)nmod * nrow;
   if (n == 0) return cudaSuccess;
-  if (nrow % 4 == 0 && ldp % 4 == 0 && slice % 4 == 0 && nmod <= 65535 &&
+  int kf = 0;
+  const bool fpow2 = factor != 0.0 && std::frexp(factor, &kf) == 0.5;  // factor = 2^(kf-1)
+  if (fpow2 && nrow % 4 == 0 && ldp % 4 == 0 && slice % 4 == 0 && nmod <= 65535 &&
       (reinterpret_cast<uintptr_t>(P) & 15) == 0) {
-    int kf = 0;
-    const bool fpow2 = factor != 0.0 && std::frexp(factor, &kf) == 0.5;  // factor = 2^(kf-1)
     if (nsplit > kPairSplits) {  // many splits: one quad per thread, 8 splits per batch
       dim3 grid(cdiv(nrow / 4, (long long)kT), nmod);
       k_splitk_reduce4<true, 1><<<grid, kT, 0, st>>>(P, nsplit, slice, nrow, ldp, rowscale,
-                                                     modscale, modmean, rowsum, fpow2, kf - 1,
-                                                     factor, out, ld_out);
+                                                     modscale, sexp, modmean, rowsum, kf - 1,
+                                                     out, ld_out);
     } else {
       dim3 grid(cdiv(nrow / 4, (long long)kT * 2), nmod);
       k_splitk_reduce4<false, 2><<<grid, kT, 0, st>>>(P, nsplit, slice, nrow, ldp, rowscale,
-                                                      modscale, modmean, rowsum, fpow2, kf - 1,
-                                                      factor, out, ld_out);
+                                                      modscale, sexp, modmean, rowsum, kf - 1,
+                                                      out, ld_out);
     }
     return cudaGetLastError();
   }
   k_splitk_reduce<<<cdiv(n, kT), kT, 0, st>>>(P, nsplit, slice, nmod, nrow, ldp, rowscale,
-                                               modscale, modmean, rowsum, factor, out, ld_out);
+                                               modscale, sexp, modmean, rowsum, factor, out,
+                                               ld_out);
   return cudaGetLastError();
 }
 

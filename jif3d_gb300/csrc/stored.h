@@ -32,17 +32,14 @@ cudaError_t launch_transpose16(const void *in, long long ld_in, long long rows, 
                                void *out, long long ld_out, cudaStream_t st);
 // FP64 [nrow][ld_src] (column c times colscale[c] when given) -> fp16 hi / lo
 // [nrow_pad][ld_dst] with a power-of-two scale per row into rowscale[r]; rows
-// beyond nrow and columns beyond ncol are zero.
-// With rowmean given, each row is centred first (rowmean[r] = its mean over
-// the ncol columns).  work: split_matrix_work(nrow_pad, ld_dst) doubles.
+// beyond nrow and columns beyond ncol are zero.  work:
+// split_matrix_work(nrow_pad, ld_dst) doubles.
 long long split_matrix_work(int nrow_pad, long long ld_dst);
-// Kernel launches of one launch_split_matrix call (1 for short rows without
-// centring, else 3).
-int split_matrix_launches(bool center, long long ld_dst);
+// Kernel launches of one launch_split_matrix call (1 for short rows, else 3).
+int split_matrix_launches(long long ld_dst);
 cudaError_t launch_split_matrix(const double *src, long long ld_src, int nrow, long long ncol,
                                 const float *colscale, void *hi, void *lo, long long ld_dst,
-                                int nrow_pad, float *rowscale, double *rowmean, double *work,
-                                cudaStream_t st);
+                                int nrow_pad, float *rowscale, double *work, cudaStream_t st);
 cudaError_t launch_to_f32(const double *src, long long n, long long npad, float *dst,
                           cudaStream_t st);
 // d[r] = sum_c J[r][c] x[c] (FP32 J, FP32 x, FP64 result), ld multiple of 4.
@@ -53,12 +50,22 @@ int gemv_t_chunks(int nrows);
 cudaError_t launch_gemv_t_f32(const float *J, long long ld, int nrows, const double *w,
                               double *part, long long ncol, double factor, double *out,
                               cudaStream_t st);
-// out[n][r] = factor * rowscale[r] * modscale[n] * sum_s P[s][n][r]  (P float, out double)
+// out[n][r] = factor * rowscale[r] * modscale[n] * sum_s 2^sexp[n][s] P[s][n][r]
+// (P float, out double; modscale and sexp optional, sexp [nmod][nsplit])
 // + modmean[n] * rowsum[r] when modmean is given (adds back a centred mean).
 cudaError_t launch_splitk_reduce(const float *P, int nsplit, long long slice, int nmod, int nrow,
                                  long long ldp, const float *rowscale, const float *modscale,
-                                 const double *modmean, const double *rowsum, double factor,
-                                 double *out, long long ld_out, cudaStream_t st);
+                                 const int *sexp, const double *modmean, const double *rowsum,
+                                 double factor, double *out, long long ld_out, cudaStream_t st);
+// Models [nrow][ld_src] (ncol values each) -> fp16 hi / lo [nrow_pad][ld_dst]
+// for the forward product with nsp K splits of cols_per_split columns, in one
+// pass: centre[r] an estimate of row r's mean (removed before the split), and
+// per split the power-of-two scale 2^sexp[r][s]: row r = centre[r] + the
+// split's 2^sexp * (hi + lo) on its columns.  Rows beyond nrow are zero.
+cudaError_t launch_split_models(const double *src, long long ld_src, int nrow, long long ncol,
+                                void *hi, void *lo, long long ld_dst, int nrow_pad,
+                                long long cols_per_split, int nsp, double *centre, int *sexp,
+                                cudaStream_t st);
 
 // Batched epilogues of the stored products (grid over station x model).
 cudaError_t launch_stored_assemble(int kind, int transform, double tbx, double tby, double tbz,
@@ -102,6 +109,8 @@ struct GemmOperands {
 };
 int gemm_n_tile(int n);
 int gemm_splits_used(long long ld, int nsplit);
+// k-blocks (64 columns) per K split: split s covers k-blocks [s kb, (s + 1) kb).
+int gemm_kb_per_split(long long ld, int nsplit);
 // P[split][n][ldp] (split stride `slice`) = per-split sums of
 // Ahi Bhi + Ahi Blo + Alo Bhi; err receives a non-zero code if a bounded
 // wait expired.

@@ -255,6 +255,69 @@ def test_pinned_gemm_plans(ctx, oracle_lib):
         ctx.set_gemm_plan(0, 4, 96)
 
 
+def test_models_split_wider_than_a_block(ctx, oracle_lib):
+    """A plan pinned to one K split over more columns than one block of the
+    models' split holds in registers (4320 cells, 68 k-blocks): the split
+    takes its two-pass form and the products still match the oracle."""
+    s = small_survey(W.JOINT, seed=310, nx=20, ny=18, nz=12, nmeas=24)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    rng = np.random.default_rng(31)
+    models = s.model[None, :] * (1 + 0.1 * rng.normal(size=(260, s.nparm)))
+    mis = rng.normal(size=(260, s.stations.shape[0] * 10))
+    try:
+        for nsplit in (1, 3):
+            ctx.set_gemm_plan(0, nsplit, 0)
+            d = ctx.batched_forward(models)
+            g = ctx.batched_lqderivative(models, mis)
+            for i in (0, 259):
+                check_groups(s, d[i], oracle_forward(oracle_lib, s, models[i]))
+                assert relerr(g[i], oracle_lqderivative(oracle_lib, s, mis[i], models[i])) <= TOL
+    finally:
+        ctx.set_gemm_plan(0, 0)
+
+
+def test_models_with_uneven_magnitudes(ctx, oracle_lib):
+    """Models whose K splits differ in magnitude by many binades (a near-zero
+    region, a large uniform part, one cell far above the rest): each split
+    takes its own scale where the row's sampled one does not bound it, and
+    the split sums bring them together exactly."""
+    s = small_survey(W.JOINT, seed=311, nx=24, ny=20, nz=10, nmeas=20)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    rng = np.random.default_rng(32)
+    ng = s.ngrid
+    models = np.tile(s.model, (6, 1))
+    models[0, :ng // 2] *= 1e-9                       # half the cells near zero
+    models[1, :ng] += 1e6                             # a large uniform part
+    models[2, 40] = 1e7                               # one outlier cell, not sampled
+    models[3, :ng] = rng.normal(size=ng) * np.logspace(-6, 6, ng)
+    models[4, :ng] = -models[4, :ng]
+    models[5, :ng] = 0.0                              # background only
+    mis = rng.normal(size=(6, s.stations.shape[0] * 10))
+    d = ctx.batched_forward(models)
+    g = ctx.batched_lqderivative(models, mis)
+    for i in range(6):
+        check_groups(s, d[i], oracle_forward(oracle_lib, s, models[i]))
+        assert relerr(g[i], oracle_lqderivative(oracle_lib, s, mis[i], models[i])) <= TOL
+
+
+def test_batched_adjoint_long_residual_rows(ctx, oracle_lib):
+    """More than 2340 joint stations (16800 stored rows): the residual weights
+    take the separate weights launch and the three-pass split of long rows."""
+    s = small_survey(W.JOINT, seed=312, nx=9, ny=8, nz=6, nmeas=2400)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    rng = np.random.default_rng(33)
+    models = s.model[None, :] * (1 + 0.1 * rng.normal(size=(3, s.nparm)))
+    mis = rng.normal(size=(3, s.stations.shape[0] * 10))
+    g = ctx.batched_lqderivative(models, mis)
+    d = ctx.batched_forward(models)
+    for i in range(3):
+        check_groups(s, d[i], oracle_forward(oracle_lib, s, models[i]))
+        assert relerr(g[i], oracle_lqderivative(oracle_lib, s, mis[i], models[i])) <= TOL
+
+
 def test_stored_is_dropped_on_new_geometry(ctx):
     s = small_survey(W.SCALAR, seed=5)
     W.setup_context(ctx, s)
