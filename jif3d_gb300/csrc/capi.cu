@@ -724,12 +724,17 @@ int stored_adjoint_f32(j3g_context *c, const double *d_model, const double *d_mi
   return zero_inert_background(c, 1, d_grad);
 }
 
-// K-splits of a tensor-core product: at most 64 k-blocks (4096 products) per
-// split keep the kernel's FP32 register sums short (the splits are added in
-// FP64), and at least about six waves of CTAs over the 152 SMs.
+// K-splits of a tensor-core product: at most kMaxKbPerSplit k-blocks per
+// split keep the kernel's FP32 register sums short (the splits are added as
+// FP32 two-sum pairs), and at least about six waves of CTAs over the 152 SMs.
+// 128 k-blocks (8192 products, 256 drained sums per register) keep every
+// output group of the config-4 products within 3e-7 of FP64 and the FTG
+// invariant's within 4e-7 (bound 1e-6); 64 gave 1e-7 / 3e-7 with twice the
+// partial sums to add.
+constexpr long long kMaxKbPerSplit = 128;
 int choose_splits(long long m, int ntiles, long long ld) {
   const long long mt = (m + 127) / 128, kb = ld / 64;
-  const long long s = std::max<long long>((kb + 63) / 64,
+  const long long s = std::max<long long>((kb + kMaxKbPerSplit - 1) / kMaxKbPerSplit,
                                           (6 * 152 + mt * ntiles - 1) / (mt * ntiles));
   return (int)std::max<long long>(1, std::min(s, kb));
 }
@@ -773,8 +778,8 @@ cudaError_t product_launches(j3g_context *c, int dir, const GemmOperands &g, int
 // fastest for the context's lifetime and reuses it.  A candidate is timed
 // as `run` queues it (nsplit, tile): the product with its split sums, and for
 // the forward the models' split, which follows the product's K splits.
-// Every candidate keeps at most 64 k-blocks per split, the bound that holds
-// the FP32 register sums to their accuracy.
+// Every candidate keeps at most kMaxKbPerSplit k-blocks per split, the bound
+// that holds the FP32 register sums to their accuracy.
 int gemm_plan(j3g_context *c, int dir, const GemmOperands &g, long long slice,
               const std::function<cudaError_t(int, int)> &run, j3g_context::GemmPlan &plan) {
   const int tile0 = gemm_n_tile((int)g.n);
@@ -798,7 +803,7 @@ int gemm_plan(j3g_context *c, int dir, const GemmOperands &g, long long slice,
   }
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-  const long long kb = g.ld / 64, smin = (kb + 63) / 64;
+  const long long kb = g.ld / 64, smin = (kb + kMaxKbPerSplit - 1) / kMaxKbPerSplit;
   std::vector<std::pair<int, int>> cand;  // (tile, nsplit)
   for (int tile : {tile0, tile0 == 256 ? 128 : 0}) {
     if (!tile || g.n_pad % tile) continue;

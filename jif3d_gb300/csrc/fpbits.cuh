@@ -82,6 +82,19 @@ __device__ __forceinline__ double scale_pow2(double d, int k) {
   return scale_pow2_mul(d, k);
 }
 
+// d * 2^k by an exponent add, branch-free: exact while the result stays a
+// normal double (then bit for bit d * 2^k); results below the normal range
+// and subnormal d become a signed zero, results above it a signed infinity;
+// infinities and NaNs pass through.
+__device__ __forceinline__ double scale_pow2_ftz(double d, int k) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned long long s = b & 0x8000000000000000ull;
+  const int e = (int)((b >> 52) & 0x7ff), ek = e + k;
+  const unsigned long long scaled =
+      ek <= 0 ? s : (ek >= 0x7ff ? (s | 0x7ff0000000000000ull) : b + ((unsigned long long)(long long)k << 52));
+  return __longlong_as_double((long long)(e == 0x7ff ? b : (e == 0 ? s : scaled)));
+}
+
 // f * 2^k by an exponent add, branch-free: exact while the result stays a
 // normal float; results below the normal range and subnormal f become a
 // signed zero, results above it a signed infinity; infinities and NaNs pass

@@ -252,16 +252,18 @@ __global__ void __launch_bounds__(kT) k_model_centre(const double *__restrict__ 
                                                      int *__restrict__ eref) {
   constexpr int kPer = kCentreRuns * kCentreRun / kT;
   const int r = blockIdx.x;
-  // run j starts at j * ncol / kCentreRuns (runs overlap when ncol is small)
+  // rows of up to kCentreRuns * kCentreRun values are taken whole; longer
+  // ones as kCentreRuns runs of kCentreRun values, run j from j * (ncol /
+  // kCentreRuns) (inside the row: ncol / kCentreRuns >= kCentreRun)
+  const long long ns = min(ncol, (long long)kCentreRuns * kCentreRun);
+  const bool whole = ncol <= (long long)kCentreRuns * kCentreRun;
   double v[kPer];
-  int cnt = 0;
 #pragma unroll
   for (int u = 0; u < kPer; ++u) {
-    const int i = threadIdx.x + u * kT, j = i / kCentreRun;
-    const long long c = (long long)j * ncol / kCentreRuns + i % kCentreRun;
-    const bool ok = r < nrow && c < ncol;
-    v[u] = ok ? src[(long long)r * ld_src + c] : 0.0;
-    cnt += ok;
+    const int i = threadIdx.x + u * kT;
+    const long long c =
+        whole ? i : (long long)(i / kCentreRun) * (ncol / kCentreRuns) + i % kCentreRun;
+    v[u] = (r < nrow && i < ns) ? src[(long long)r * ld_src + c] : 0.0;
   }
   double s = 0.0;
 #pragma unroll
@@ -269,13 +271,13 @@ __global__ void __launch_bounds__(kT) k_model_centre(const double *__restrict__ 
   __shared__ double red[kT / 32];
   __shared__ double sh_c;
   s = block_sum_d<kT>(s, red);
-  const double n = block_sum_d<kT>((double)cnt, red);
-  if (threadIdx.x == 0) sh_c = n > 0.0 ? s / n : 0.0;
+  if (threadIdx.x == 0) sh_c = ns > 0 ? s / (double)ns : 0.0;
   __syncthreads();
   const float c32 = approx_f32(sh_c);
   float mf = 0.0f;
 #pragma unroll
-  for (int u = 0; u < kPer; ++u) mf = fmaxf(mf, fabsf(approx_f32(v[u]) - c32));
+  for (int u = 0; u < kPer; ++u)
+    if (threadIdx.x + u * kT < ns) mf = fmaxf(mf, fabsf(approx_f32(v[u]) - c32));
   const double m = warp_max_d((double)mf);
   __syncthreads();
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
@@ -292,17 +294,37 @@ __global__ void __launch_bounds__(kT) k_model_centre(const double *__restrict__ 
   }
 }
 
-// One block per (model row, K split): d = v - centre (the one FP64 operation
-// per element), rounded to float and kept in registers; the split's exponent
-// e = max(eref[row], frexp exponent of max |d| - 14) (sexp[row][split]), so
-// |d| / 2^e < 2^14; then hi + lo of d / 2^e (a float multiply by a power of
-// two: exact, one rounding in all, for the exponents of any physical model;
-// others take the FP64 scaling).  Splits of up to kT * kSplitPer columns
-// keep the values in registers; wider ones (plans pinned past the accuracy
-// bound, WIDE) compute them again in the second pass.
+// v - c in float arithmetic, for a double v and a centre c = ch + cl given as
+// a float pair: v = vh + vl with vh its sign, exponent and leading 20
+// fraction bits (exact) and vl its low 32 fraction bits (rounded to float),
+// d = (vh - ch) + (vl - cl), accurate to about 2^-23 |d| + 2^-44 |v| with no
+// FP64 operation.  |v| below 2^-126 counts as zero; bad is set for |v| of
+// 2^128 or more (and infinities, NaNs), which the caller takes in FP64.
+__device__ __forceinline__ float centred_f32(double v, float ch, float cl, bool &bad) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const uint32_t h = (uint32_t)(b >> 32), l = (uint32_t)b;
+  const uint32_t s = h & 0x80000000u, e = (h >> 20) & 0x7ffu;
+  bad |= e >= 1151u;
+  const bool tiny = e <= 896u;
+  const float vh = __uint_as_float(tiny ? s : (s | ((e - 896u) << 23) | ((h & 0xfffffu) << 3)));
+  const int pe = (int)e - 948;  // biased float exponent of 2^(e - 1075)
+  const float vl = (!tiny && pe > 0)
+                       ? __uint2float_rn(l) * __uint_as_float(s | ((uint32_t)pe << 23))
+                       : 0.0f;
+  return __fadd_rn(__fsub_rn(vh, ch), __fsub_rn(vl, cl));
+}
+
+// One block per (model row, K split): d = v - centre in float arithmetic
+// (centred_f32) kept in registers; the split's exponent e = max(eref[row],
+// frexp exponent of max |d| - 14) (sexp[row][split]), so |d| / 2^e < 2^14;
+// then hi + lo of d / 2^e (a float multiply by a power of two, exact).  A
+// split with a value beyond the float range, an exponent outside
+// [-100, 100], or more columns than kT * kSplitPer (plans pinned past the
+// accuracy bound, WIDE) is computed in FP64 instead: d = v - centre, then
+// one rounding of d / 2^e to float.
 constexpr int kSplitPer = 16;
 template <bool WIDE>
-__global__ void __launch_bounds__(kT) k_split_models(
+__global__ void __launch_bounds__(kT, 4) k_split_models(
     const double *__restrict__ src, long long ld_src, int nrow, long long ncol,
     const double *__restrict__ centre, const int *__restrict__ eref, __half *__restrict__ hi,
     __half *__restrict__ lo, long long ld_dst, long long cols_per_split, int nsp,
@@ -313,24 +335,33 @@ __global__ void __launch_bounds__(kT) k_split_models(
   const bool row_ok = r < nrow;
   const double cr = row_ok ? centre[r] : 0.0;
   const double *row = src + r * ld_src;
-  constexpr bool in_regs = !WIDE;
+  auto in_row = [&](long long c) { return row_ok && c < c1 && c < ncol; };
   float x[kSplitPer];
   float mf = 0.0f;
-  if constexpr (in_regs) {
-    double v[kSplitPer];
+  bool bad = WIDE;
+  if constexpr (!WIDE) {
+    const float ch = f64_to_f32_ftz(cr), cl = f64_to_f32_ftz(cr - (double)ch);
 #pragma unroll
-    for (int u = 0; u < kSplitPer; ++u) {
-      const long long c = c0 + threadIdx.x + (long long)u * kT;
-      v[u] = (row_ok && c < c1 && c < ncol) ? row[c] : cr;
-    }
+    for (int h0 = 0; h0 < kSplitPer; h0 += 8) {
+      double v[8];  // a batch of loads in flight
 #pragma unroll
-    for (int u = 0; u < kSplitPer; ++u) {
-      x[u] = f64_to_f32_ftz(v[u] - cr);
-      mf = fmaxf(mf, fabsf(x[u]));
+      for (int u = 0; u < 8; ++u) {
+        const long long c = c0 + threadIdx.x + (long long)(h0 + u) * kT;
+        v[u] = in_row(c) ? row[c] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const long long c = c0 + threadIdx.x + (long long)(h0 + u) * kT;
+        x[h0 + u] = in_row(c) ? centred_f32(v[u], ch, cl, bad) : 0.0f;
+        mf = fmaxf(mf, fabsf(x[h0 + u]));
+      }
     }
-  } else {
+  }
+  const bool fp64 = __syncthreads_or(bad) != 0;
+  if (fp64) {
+    mf = 0.0f;
     for (long long c = c0 + threadIdx.x; c < c1; c += kT)
-      if (row_ok && c < ncol) mf = fmaxf(mf, fabsf(f64_to_f32_ftz(row[c] - cr)));
+      if (in_row(c)) mf = fmaxf(mf, fabsf(f64_to_f32_ftz(row[c] - cr)));
   }
   __shared__ float red[kT / 32];
   __shared__ int sh_e;
@@ -352,36 +383,24 @@ __global__ void __launch_bounds__(kT) k_split_models(
   }
   __syncthreads();
   const int e = sh_e;
-  const bool fast = e >= -100 && e <= 100;  // float scaling exact, no overflow
-  const float inv = fast ? __uint_as_float((uint32_t)(127 - e) << 23) : 0.0f;
-  // 2^-e as a double (the split exponents of finite doubles stay within
-  // -1100 .. 1040; beyond the normal range the scaling saturates)
-  const int eb = min(2046, max(1, 1023 - e));
-  const double inv64 = __longlong_as_double((long long)eb << 52);
-  auto put = [&](long long c, float xf, double dv) {
-    const float xs = fast ? xf * inv : f64_to_f32_ftz(dv * inv64);
+  auto put = [&](long long c, float xs) {
     const __half hv = __float2half_rn(xs);
     hi[r * ld_dst + c] = hv;
     lo[r * ld_dst + c] = __float2half_rn(__fsub_rn(xs, __half2float(hv)));
   };
-  if constexpr (in_regs) {
-    if (fast) {
+  if (!fp64 && e >= -100 && e <= 100) {
+    const float inv = __uint_as_float((uint32_t)(127 - e) << 23);  // 2^-e
 #pragma unroll
-      for (int u = 0; u < kSplitPer; ++u) {
-        const long long c = c0 + threadIdx.x + (long long)u * kT;
-        if (c < c1) put(c, x[u], 0.0);
-      }
-    } else {
-      for (int u = 0; u < kSplitPer; ++u) {
-        const long long c = c0 + threadIdx.x + (long long)u * kT;
-        if (c < c1) put(c, 0.0f, (row_ok && c < ncol) ? row[c] - cr : 0.0);
-      }
+    for (int u = 0; u < kSplitPer; ++u) {
+      const long long c = c0 + threadIdx.x + (long long)u * kT;
+      if (c < c1) put(c, x[u] * inv);
     }
   } else {
-    for (long long c = c0 + threadIdx.x; c < c1; c += kT) {
-      const double dv = (row_ok && c < ncol) ? row[c] - cr : 0.0;
-      put(c, f64_to_f32_ftz(dv), dv);
-    }
+    // 2^-e as a double (split exponents of finite doubles stay within
+    // -1100 .. 1040; beyond the normal range the scaling saturates)
+    const double inv64 = __longlong_as_double((long long)min(2046, max(1, 1023 - e)) << 52);
+    for (long long c = c0 + threadIdx.x; c < c1; c += kT)
+      put(c, in_row(c) ? f64_to_f32_ftz((row[c] - cr) * inv64) : 0.0f);
   }
 }
 
@@ -600,7 +619,7 @@ __global__ void __launch_bounds__(kT) k_splitk_reduce4(
     const float *__restrict__ rowscale, const float *__restrict__ modscale,
     const int *__restrict__ sexp, const double *__restrict__ modmean,
     const double *__restrict__ rowsum, int kfac, double *__restrict__ out, long long ld_out) {
-  constexpr int U = G == 1 ? 8 : 2;
+  constexpr int U = G == 1 ? 4 : 2;
   const int nq = nrow / 4;
   const int n = blockIdx.y;
   // per-split scales 2^sexp[n][s]: each split's partials are brought to the
@@ -891,7 +910,8 @@ k_weights_split(int transform, double tbx, double tby, double tbz, int nmeas, in
       stored_weights<kind>(w, mf, v[k]);
 #pragma unroll
       for (int q = 0; q < ns; ++q) {
-        v[k][q] = v[k][q] * (double)colscale[(long long)s * ns + q];
+        // times J's row scale, a power of two: an exponent add
+        v[k][q] = scale_pow2_ftz(v[k][q], pow2_exponent(colscale[(long long)s * ns + q]));
         mf32 = fmaxf(mf32, fabsf(approx_f32(v[k][q])));
       }
     }
@@ -908,7 +928,7 @@ k_weights_split(int transform, double tbx, double tby, double tbz, int nmeas, in
     rowscale[n] = sh_scale;
   }
   __syncthreads();
-  const double inv = 1.0 / (double)sh_scale;  // a power of two: exact
+  const int kinv = -pow2_exponent(sh_scale);  // dividing by the scale: an exponent add
   __half *h = hi + (long long)n * ld_dst;
   __half *l = lo + (long long)n * ld_dst;
 #pragma unroll
@@ -917,7 +937,7 @@ k_weights_split(int transform, double tbx, double tby, double tbz, int nmeas, in
     if (s < nmeas) {
 #pragma unroll
       for (int q = 0; q < ns; ++q) {
-        const float x = n < nmod ? f64_to_f32_ftz(fma(v[k][q], inv, 0.0)) : 0.0f;
+        const float x = n < nmod ? f64_to_f32_ftz(scale_pow2_ftz(v[k][q], kinv)) : 0.0f;
         const __half hv = __float2half_rn(x);
         h[(long long)s * ns + q] = hv;
         l[(long long)s * ns + q] = __float2half_rn(__fsub_rn(x, __half2float(hv)));
