@@ -339,13 +339,13 @@ int j3g_get_timing(j3g_context *ctx, int category, double *total_ms, long long *
 
 /* Autotuning of the tensor-core products (J3G_STORE_F16X2 batched calls); no
  * reference counterpart.  Off by default: a fixed rule picks the K-split count
- * and the N tile (about six waves of CTAs, at most 64 k-blocks per split), so
+ * and the N tile (about six waves of CTAs, at most 128 k-blocks per split), so
  * a caller that never calls this -- the unchanged jif3D calculators through
  * the C++ implementation, for one -- runs untuned plans.  With enable = 1, the first product of each shape (direction,
  * rows, models, K) times a few candidate plans -- split counts that fill the
  * last wave of CTAs, and one-SM 128-wide tiles in place of CTA pairs -- and
  * keeps the fastest for the context's lifetime.  Every candidate keeps the
- * accuracy bound of the fixed rule (at most 64 k-blocks per split).  Tuning
+ * accuracy bound of the fixed rule (at most 128 k-blocks per split).  Tuning
  * synchronises the context's stream, so the first call of a shape must not be
  * made while the stream is being captured into a CUDA graph; results can
  * differ from the fixed plan's in the last bits (another summation order). */
@@ -354,7 +354,7 @@ int j3g_set_autotune(j3g_context *ctx, int enable);
  * (0 = by the number of models, 64, 128, 256; a tile the batch does not fill
  * falls back to the automatic plan).  nsplit <= 0 returns to the fixed rule or
  * the autotuner.  For reproducible runs with a plan found by tuning; more
- * than 64 k-blocks per split loses accuracy (the split sums are FP32). */
+ * than 128 k-blocks per split loses accuracy (the split sums are FP32). */
 int j3g_set_gemm_plan(j3g_context *ctx, int direction, int nsplit, int tile);
 /* The plan the last batched product used: direction 0 forward (J M), 1
  * adjoint (J^T R); K splits requested, N tile (64, 128 or 256 = CTA pair) and

@@ -321,10 +321,11 @@ __device__ __forceinline__ float centred_f32(double v, float ch, float cl, bool 
 // split with a value beyond the float range, an exponent outside
 // [-100, 100], or more columns than kT * kSplitPer (plans pinned past the
 // accuracy bound, WIDE) is computed in FP64 instead: d = v - centre, then
-// one rounding of d / 2^e to float.
+// one rounding of d / 2^e to float.  NT threads a block: 256 for splits of up
+// to 4096 columns, 512 up to 8192.
 constexpr int kSplitPer = 16;
-template <bool WIDE>
-__global__ void __launch_bounds__(kT, 4) k_split_models(
+template <bool WIDE, int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) k_split_models(
     const double *__restrict__ src, long long ld_src, int nrow, long long ncol,
     const double *__restrict__ centre, const int *__restrict__ eref, __half *__restrict__ hi,
     __half *__restrict__ lo, long long ld_dst, long long cols_per_split, int nsp,
@@ -346,12 +347,12 @@ __global__ void __launch_bounds__(kT, 4) k_split_models(
       double v[8];  // a batch of loads in flight
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        const long long c = c0 + threadIdx.x + (long long)(h0 + u) * kT;
+        const long long c = c0 + threadIdx.x + (long long)(h0 + u) * NT;
         v[u] = in_row(c) ? row[c] : 0.0;
       }
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        const long long c = c0 + threadIdx.x + (long long)(h0 + u) * kT;
+        const long long c = c0 + threadIdx.x + (long long)(h0 + u) * NT;
         x[h0 + u] = in_row(c) ? centred_f32(v[u], ch, cl, bad) : 0.0f;
         mf = fmaxf(mf, fabsf(x[h0 + u]));
       }
@@ -360,10 +361,10 @@ __global__ void __launch_bounds__(kT, 4) k_split_models(
   const bool fp64 = __syncthreads_or(bad) != 0;
   if (fp64) {
     mf = 0.0f;
-    for (long long c = c0 + threadIdx.x; c < c1; c += kT)
+    for (long long c = c0 + threadIdx.x; c < c1; c += NT)
       if (in_row(c)) mf = fmaxf(mf, fabsf(f64_to_f32_ftz(row[c] - cr)));
   }
-  __shared__ float red[kT / 32];
+  __shared__ float red[NT / 32];
   __shared__ int sh_e;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mf = fmaxf(mf, __shfl_down_sync(0xffffffffu, mf, o));
@@ -371,7 +372,7 @@ __global__ void __launch_bounds__(kT, 4) k_split_models(
   __syncthreads();
   if (threadIdx.x == 0) {
     float m = 0.0f;
-    for (int w = 0; w < kT / 32; ++w) m = fmaxf(m, red[w]);
+    for (int w = 0; w < NT / 32; ++w) m = fmaxf(m, red[w]);
     // m in [2^(E-1), 2^E) with E = biased exponent - 126; rounding to float
     // can lift a maximum just below 2^E to 2^E, which only raises E
     const uint32_t be = (__float_as_uint(m) >> 23) & 0xffu;
@@ -392,14 +393,14 @@ __global__ void __launch_bounds__(kT, 4) k_split_models(
     const float inv = __uint_as_float((uint32_t)(127 - e) << 23);  // 2^-e
 #pragma unroll
     for (int u = 0; u < kSplitPer; ++u) {
-      const long long c = c0 + threadIdx.x + (long long)u * kT;
+      const long long c = c0 + threadIdx.x + (long long)u * NT;
       if (c < c1) put(c, x[u] * inv);
     }
   } else {
     // 2^-e as a double (split exponents of finite doubles stay within
     // -1100 .. 1040; beyond the normal range the scaling saturates)
     const double inv64 = __longlong_as_double((long long)min(2046, max(1, 1023 - e)) << 52);
-    for (long long c = c0 + threadIdx.x; c < c1; c += kT)
+    for (long long c = c0 + threadIdx.x; c < c1; c += NT)
       put(c, in_row(c) ? f64_to_f32_ftz((row[c] - cr) * inv64) : 0.0f);
   }
 }
@@ -873,13 +874,20 @@ k_stored_weights(int transform, double tbx, double tby, double tbz, int nmeas,
 
 // The stored-row weights of one model and their fp16 split in one launch, for
 // surveys of at most kWsThreads * kWsPer stations: block n computes every
-// station's weights in registers (k_stored_weights' arithmetic, raw-row
-// weights written to w_raw), scales them by J's row scales, takes the row's
-// maximum and splits them (k_split_rows_small's arithmetic) -- the same
-// values as the two launches, without the weights' round trip through HBM.
+// station's weights (k_stored_weights' arithmetic, raw-row weights written to
+// w_raw), scales them by J's row scales, takes the row's maximum and splits
+// them (k_split_rows_small's arithmetic) -- the same values as the two
+// launches, without the weights' round trip through HBM.  The stations'
+// records move through shared memory (the misfit and raw-weight records of
+// kWsThreads stations at a time, the scaled stored weights of all), so that
+// every global access is coalesced and the split runs one thread per element.
 // Rows n >= nmod are zero padding (scale 1), as in the split.
 constexpr int kWsThreads = 512;
 constexpr int kWsPer = 2;
+template <int KIND>
+constexpr int weights_split_smem() {
+  return (kWsThreads * kind_raw(KIND) + kWsThreads * kWsPer * stored_rows(KIND)) * 8;
+}
 template <int KIND>
 __global__ void __launch_bounds__(kWsThreads)
 k_weights_split(int transform, double tbx, double tby, double tbz, int nmeas, int nmod,
@@ -890,38 +898,47 @@ k_weights_split(int transform, double tbx, double tby, double tbz, int nmeas, in
   constexpr int kind = KIND;
   constexpr int raw = kind_raw(kind);
   constexpr int ns = stored_rows(kind);
-  const int n = blockIdx.x;
-  double v[kWsPer][ns];
+  extern __shared__ double ws_smem[];
+  double *rec = ws_smem;                       // [kWsThreads][raw]: misfit, then raw weights
+  double *stw = ws_smem + kWsThreads * raw;    // [nmeas][ns]: scaled stored weights
+  const int n = blockIdx.x, t = threadIdx.x;
+  const bool live = n < nmod;
+  const bool plain = transform == TR_NONE;
+  const double *mis = misfit + (long long)n * ld_misfit;
+  double *wr_row = w_raw + (long long)n * nmeas * raw;
   float mf32 = 0.0f;
-#pragma unroll
-  for (int k = 0; k < kWsPer; ++k) {
-    const int s = threadIdx.x + k * kWsThreads;
-    if (n < nmod && s < nmeas) {
-      const double *mis = misfit + n * ld_misfit;
-      const bool plain = transform == TR_NONE;
-      double w[10];
-      station_weights<raw>(transform, tbx, tby, tbz, mis + (long long)s * raw,
-                           plain ? 0.0 : mis[s],
+  for (int s0 = 0; s0 < nmeas; s0 += kWsThreads) {
+    const int count = min(kWsThreads, nmeas - s0), s = s0 + t;
+    if (live && plain) copy_records<raw>(rec, mis + (long long)s0 * raw, count);
+    __syncthreads();
+    if (live && t < count) {
+      double w[10], v[ns];
+      station_weights<raw>(transform, tbx, tby, tbz, rec + t * raw, plain ? 0.0 : mis[s],
                            plain ? nullptr : rawd + (long long)n * nmeas * raw + (long long)s * raw,
                            w);
-      double *wr = w_raw + (long long)n * nmeas * raw + (long long)s * raw;
+      if (!plain) {
 #pragma unroll
-      for (int c = 0; c < raw; ++c) wr[c] = w[c];
-      stored_weights<kind>(w, mf, v[k]);
+        for (int c = 0; c < raw; ++c) rec[t * raw + c] = w[c];
+      }
+      stored_weights<kind>(w, mf, v);
 #pragma unroll
       for (int q = 0; q < ns; ++q) {
         // times J's row scale, a power of two: an exponent add
-        v[k][q] = scale_pow2_ftz(v[k][q], pow2_exponent(colscale[(long long)s * ns + q]));
-        mf32 = fmaxf(mf32, fabsf(approx_f32(v[k][q])));
+        const double x = scale_pow2_ftz(v[q], pow2_exponent(colscale[(long long)s * ns + q]));
+        stw[s * ns + q] = x;
+        mf32 = fmaxf(mf32, fabsf(approx_f32(x)));
       }
     }
+    __syncthreads();
+    if (live) copy_records<raw>(wr_row + (long long)s0 * raw, rec, count);
+    __syncthreads();
   }
   __shared__ double red[kWsThreads / 32];
   __shared__ float sh_scale;
   const double m = warp_max_d((double)mf32);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  if ((t & 31) == 0) red[t >> 5] = m;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (t == 0) {
     double mm = 0.0;
     for (int w = 0; w < kWsThreads / 32; ++w) mm = fmax(mm, red[w]);
     sh_scale = (float)pow2_scale(mm);
@@ -931,21 +948,15 @@ k_weights_split(int transform, double tbx, double tby, double tbz, int nmeas, in
   const int kinv = -pow2_exponent(sh_scale);  // dividing by the scale: an exponent add
   __half *h = hi + (long long)n * ld_dst;
   __half *l = lo + (long long)n * ld_dst;
-#pragma unroll
-  for (int k = 0; k < kWsPer; ++k) {
-    const int s = threadIdx.x + k * kWsThreads;
-    if (s < nmeas) {
-#pragma unroll
-      for (int q = 0; q < ns; ++q) {
-        const float x = n < nmod ? f64_to_f32_ftz(scale_pow2_ftz(v[k][q], kinv)) : 0.0f;
-        const __half hv = __float2half_rn(x);
-        h[(long long)s * ns + q] = hv;
-        l[(long long)s * ns + q] = __float2half_rn(__fsub_rn(x, __half2float(hv)));
-      }
-    }
+  const int nel = nmeas * ns;
+  for (int i = t; i < nel; i += kWsThreads) {
+    const float x = live ? f64_to_f32_ftz(scale_pow2_ftz(stw[i], kinv)) : 0.0f;
+    const __half hv = __float2half_rn(x);
+    h[i] = hv;
+    l[i] = __float2half_rn(__fsub_rn(x, __half2float(hv)));
   }
   // padding columns
-  for (long long c = (long long)nmeas * ns + threadIdx.x; c < ld_dst; c += kWsThreads) {
+  for (long long c = (long long)nel + t; c < ld_dst; c += kWsThreads) {
     h[c] = __float2half_rn(0.0f);
     l[c] = __float2half_rn(0.0f);
   }
@@ -1035,16 +1046,16 @@ cudaError_t launch_split_models(const double *src, long long ld_src, int nrow, l
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   dim3 grid(nsp, nrow_pad);
-  if (cols_per_split <= (long long)kT * kSplitPer)
-    k_split_models<false><<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, centre, eref,
-                                               static_cast<__half *>(hi),
-                                               static_cast<__half *>(lo), ld_dst,
-                                               cols_per_split, nsp, sexp);
+  __half *h = static_cast<__half *>(hi), *l = static_cast<__half *>(lo);
+  if (cols_per_split <= 256LL * kSplitPer)
+    k_split_models<false, 256><<<grid, 256, 0, st>>>(src, ld_src, nrow, ncol, centre, eref, h, l,
+                                                     ld_dst, cols_per_split, nsp, sexp);
+  else if (cols_per_split <= 512LL * kSplitPer)
+    k_split_models<false, 512><<<grid, 512, 0, st>>>(src, ld_src, nrow, ncol, centre, eref, h, l,
+                                                     ld_dst, cols_per_split, nsp, sexp);
   else
-    k_split_models<true><<<grid, kT, 0, st>>>(src, ld_src, nrow, ncol, centre, eref,
-                                              static_cast<__half *>(hi),
-                                              static_cast<__half *>(lo), ld_dst, cols_per_split,
-                                              nsp, sexp);
+    k_split_models<true, 512><<<grid, 512, 0, st>>>(src, ld_src, nrow, ncol, centre, eref, h, l,
+                                                    ld_dst, cols_per_split, nsp, sexp);
   return cudaGetLastError();
 }
 
@@ -1163,9 +1174,14 @@ cudaError_t launch_weights_split(int kind, int transform, double tbx, double tby
   if (!weights_split_fits(nmeas, ld_dst, nrow_pad)) return cudaErrorInvalidValue;
   if ((long long)nmeas * stored_rows(kind) > ld_dst) return cudaErrorInvalidValue;
 #define J3G_WS(K)                                                                             \
-  k_weights_split<K><<<nrow_pad, kWsThreads, 0, st>>>(                                        \
-      transform, tbx, tby, tbz, nmeas, nmod, misfit, ld_misfit, rawd, mf, w_raw, colscale,     \
-      rowscale, static_cast<__half *>(hi), static_cast<__half *>(lo), ld_dst)
+  do {                                                                                        \
+    const cudaError_t ea = allow_smem_once(reinterpret_cast<const void *>(k_weights_split<K>),    \
+                                              weights_split_smem<K>());                       \
+    if (ea != cudaSuccess) return ea;                                                         \
+    k_weights_split<K><<<nrow_pad, kWsThreads, weights_split_smem<K>(), st>>>(                \
+        transform, tbx, tby, tbz, nmeas, nmod, misfit, ld_misfit, rawd, mf, w_raw, colscale,   \
+        rowscale, static_cast<__half *>(hi), static_cast<__half *>(lo), ld_dst);               \
+  } while (0)
   switch (kind) {
     case KIND_SCALAR: J3G_WS(KIND_SCALAR); break;
     case KIND_TENSOR: J3G_WS(KIND_TENSOR); break;
