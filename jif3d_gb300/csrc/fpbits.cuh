@@ -82,6 +82,20 @@ __device__ __forceinline__ double scale_pow2(double d, int k) {
   return scale_pow2_mul(d, k);
 }
 
+// scale_pow2(f32_to_f64(f), k), bit for bit: a normal float whose scaled
+// double stays normal takes one exponent rebias (a few integer operations);
+// zeros, subnormals, infinities, NaNs and out-of-range results take the
+// general path.
+__device__ __forceinline__ double widen_pow2(float f, int k) {
+  const uint32_t u = __float_as_uint(f), e = (u >> 23) & 0xffu;
+  const int eb = (int)e + 896 + k;  // biased exponent of the result
+  if (e - 1u < 254u && eb > 0 && eb < 0x7ff)
+    return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
+                                            ((unsigned long long)eb << 52) |
+                                            ((unsigned long long)(u & 0x7fffffu) << 29)));
+  return scale_pow2(f32_to_f64(f), k);
+}
+
 // d * 2^k by an exponent add, branch-free: exact while the result stays a
 // normal double (then bit for bit d * 2^k); results below the normal range
 // and subnormal d become a signed zero, results above it a signed infinity;

@@ -340,20 +340,27 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_split_models(
   float x[kSplitPer];
   float mf = 0.0f;
   bool bad = WIDE;
+  // in registers, each thread holds column pairs (c, c + 1), c = c0 + 2 (t + u NT):
+  // x[2u], x[2u + 1] (c0 and the split ends are multiples of 64, so a pair
+  // never straddles them)
   if constexpr (!WIDE) {
     const float ch = f64_to_f32_ftz(cr), cl = f64_to_f32_ftz(cr - (double)ch);
+    // columns of this thread relative to c0, and the end of the row's values
+    const int j0 = 2 * (int)threadIdx.x;
+    const int jend = row_ok ? (int)(min(c1, ncol) - c0) : 0;
+    const double *rp = row + c0;
 #pragma unroll
     for (int h0 = 0; h0 < kSplitPer; h0 += 8) {
       double v[8];  // a batch of loads in flight
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        const long long c = c0 + threadIdx.x + (long long)(h0 + u) * NT;
-        v[u] = in_row(c) ? row[c] : 0.0;
+        const int j = j0 + ((h0 + u) >> 1) * 2 * NT + (u & 1);
+        v[u] = j < jend ? rp[j] : 0.0;
       }
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        const long long c = c0 + threadIdx.x + (long long)(h0 + u) * NT;
-        x[h0 + u] = in_row(c) ? centred_f32(v[u], ch, cl, bad) : 0.0f;
+        const int j = j0 + ((h0 + u) >> 1) * 2 * NT + (u & 1);
+        x[h0 + u] = j < jend ? centred_f32(v[u], ch, cl, bad) : 0.0f;
         mf = fmaxf(mf, fabsf(x[h0 + u]));
       }
     }
@@ -391,10 +398,19 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_split_models(
   };
   if (!fp64 && e >= -100 && e <= 100) {
     const float inv = __uint_as_float((uint32_t)(127 - e) << 23);  // 2^-e
+    const int jn = (int)(c1 - c0);
+    __half2 *hp = reinterpret_cast<__half2 *>(hi + r * ld_dst + c0);
+    __half2 *lp = reinterpret_cast<__half2 *>(lo + r * ld_dst + c0);
 #pragma unroll
-    for (int u = 0; u < kSplitPer; ++u) {
-      const long long c = c0 + threadIdx.x + (long long)u * NT;
-      if (c < c1) put(c, x[u] * inv);
+    for (int u = 0; u < kSplitPer; u += 2) {
+      const int p = (int)threadIdx.x + (u >> 1) * NT;  // column pair 2p, 2p + 1
+      if (2 * p < jn) {  // one 4-byte store per part
+        const float x0 = x[u] * inv, x1 = x[u + 1] * inv;
+        const __half2 hv = __floats2half2_rn(x0, x1);
+        const float2 hf = __half22float2(hv);
+        hp[p] = hv;
+        lp[p] = __floats2half2_rn(__fsub_rn(x0, hf.x), __fsub_rn(x1, hf.y));
+      }
     }
   } else {
     // 2^-e as a double (split exponents of finite doubles stay within
@@ -711,9 +727,9 @@ __global__ void __launch_bounds__(kT) k_splitk_reduce4(
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       // a compile-time choice: as a run-time select both arms were evaluated
-      double v = PAIR ? f32_to_f64(hi[g][i]) + f32_to_f64(lo[g][i])
-                      : f32_to_f64(__fadd_rn(hi[g][i], lo[g][i]));
-      v = scale_pow2(v, kmod + (rowscale ? pow2_exponent(rowscale[r + i]) : 0));
+      const int k = kmod + (rowscale ? pow2_exponent(rowscale[r + i]) : 0);
+      double v = PAIR ? scale_pow2(f32_to_f64(hi[g][i]) + f32_to_f64(lo[g][i]), k)
+                      : widen_pow2(__fadd_rn(hi[g][i], lo[g][i]), k);
       if (modmean) v = fma(modmean[n], scale_pow2(rowsum[r + i], kfac), v);
       res[i] = v;
     }
