@@ -967,7 +967,7 @@ int batched_adjoint_pass(j3g_context *c, int nmod, const double *d_models,
   J3G_TRY(ensure(c, c->wrawb, sizeof(double) * (size_t)nmod * c->nmeas * raw));
   const int tile = gemm_n_tile(nmod);
   const long long npad = (nmod + tile - 1) / tile * tile;
-  // fp16 products on a survey that fits one block per model: the weights and
+  // fp16 products on a survey that fits one cluster per model: the weights and
   // their split in one launch (the same values as the two launches below)
   const bool fused = c->storage != J3G_STORE_FP32 && weights_split_fits(c->nmeas, ldR, (int)npad);
   if (!fused) {

@@ -14,6 +14,7 @@
 //                              the K-major operand of the adjoint GEMM.
 // Streaming products accumulate in FP32 in short chains and in FP64 across
 // chains; the tensor-core products are in gemm_tc.cu.
+#include <cooperative_groups.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -254,43 +255,56 @@ __global__ void __launch_bounds__(kT) k_model_centre(const double *__restrict__ 
   const int r = blockIdx.x;
   // rows of up to kCentreRuns * kCentreRun values are taken whole; longer
   // ones as kCentreRuns runs of kCentreRun values, run j from j * (ncol /
-  // kCentreRuns) (inside the row: ncol / kCentreRuns >= kCentreRun)
+  // kCentreRuns) (inside the row: ncol / kCentreRuns >= kCentreRun).  The
+  // estimates run in float on truncated values (the FP64 pipe would be the
+  // slowest part of this short kernel): the centre only has to be near the
+  // row's values, and the scale needs only the binade of their spread.
   const long long ns = min(ncol, (long long)kCentreRuns * kCentreRun);
   const bool whole = ncol <= (long long)kCentreRuns * kCentreRun;
-  double v[kPer];
+  float v[kPer];
 #pragma unroll
   for (int u = 0; u < kPer; ++u) {
     const int i = threadIdx.x + u * kT;
     const long long c =
         whole ? i : (long long)(i / kCentreRun) * (ncol / kCentreRuns) + i % kCentreRun;
-    v[u] = (r < nrow && i < ns) ? src[(long long)r * ld_src + c] : 0.0;
+    v[u] = (r < nrow && i < ns) ? approx_f32(src[(long long)r * ld_src + c]) : 0.0f;
   }
-  double s = 0.0;
+  float s = 0.0f;
 #pragma unroll
   for (int u = 0; u < kPer; ++u) s += v[u];
-  __shared__ double red[kT / 32];
-  __shared__ double sh_c;
-  s = block_sum_d<kT>(s, red);
-  if (threadIdx.x == 0) sh_c = ns > 0 ? s / (double)ns : 0.0;
+  __shared__ float red[kT / 32];
+  __shared__ float sh_c;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
   __syncthreads();
-  const float c32 = approx_f32(sh_c);
+  if (threadIdx.x == 0) {
+    float a = 0.0f;
+    for (int w = 0; w < kT / 32; ++w) a += red[w];
+    // values beyond the float range make the estimate infinite: centre 0
+    // (the split takes such values in FP64)
+    sh_c = (ns > 0 && isfinite(a)) ? a / (float)ns : 0.0f;
+  }
+  __syncthreads();
+  const float c32 = sh_c;
   float mf = 0.0f;
 #pragma unroll
   for (int u = 0; u < kPer; ++u)
-    if (threadIdx.x + u * kT < ns) mf = fmaxf(mf, fabsf(approx_f32(v[u]) - c32));
-  const double m = warp_max_d((double)mf);
+    if (threadIdx.x + u * kT < ns) mf = fmaxf(mf, fabsf(v[u] - c32));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mf = fmaxf(mf, __shfl_down_sync(0xffffffffu, mf, o));
   __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mf;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double mm = 0.0;
-    for (int w = 0; w < kT / 32; ++w) mm = fmax(mm, red[w]);
-    centre[r] = sh_c;
-    // frexp exponent of the sampled maximum, minus 14, plus the margin; an
-    // all-equal sample leaves it to the splits' own maxima
-    int e = 0;
-    if (mm > 0.0) frexp(mm, &e);
-    eref[r] = mm > 0.0 ? e - 14 + kScaleMargin : INT_MIN / 2;
+    float m = 0.0f;
+    for (int w = 0; w < kT / 32; ++w) m = fmaxf(m, red[w]);
+    centre[r] = (double)c32;
+    // frexp exponent of the sampled maximum (m in [2^(E-1), 2^E), E = biased
+    // exponent - 126), minus 14, plus the margin; an all-equal (or
+    // subnormal) sample leaves the scale to the splits' own maxima
+    const uint32_t be = (__float_as_uint(m) >> 23) & 0xffu;
+    eref[r] = be ? (int)be - 126 - 14 + kScaleMargin : INT_MIN / 2;
   }
 }
 
@@ -755,9 +769,26 @@ __global__ void __launch_bounds__(kT) k_splitk_reduce4(
 // memory: coalesced reads and writes instead of one strided access per value.
 constexpr int kAsm = 128;
 
+// count records of W doubles, src to dst, by the whole block: each thread
+// issues a batch of kCopyBatch loads before it stores them, so that a copy
+// from global memory costs one round trip per batch instead of one per value.
+constexpr int kCopyBatch = 8;
 template <int W>
 __device__ __forceinline__ void copy_records(double *dst, const double *src, int count) {
-  for (int i = threadIdx.x; i < count * W; i += blockDim.x) dst[i] = src[i];
+  const int n = count * W, nt = blockDim.x;
+  for (int i0 = threadIdx.x; i0 < n; i0 += nt * kCopyBatch) {
+    double v[kCopyBatch];
+#pragma unroll
+    for (int u = 0; u < kCopyBatch; ++u) {
+      const int i = i0 + u * nt;
+      v[u] = i < n ? src[i] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < kCopyBatch; ++u) {
+      const int i = i0 + u * nt;
+      if (i < n) dst[i] = v[u];
+    }
+  }
 }
 
 template <int KIND>
@@ -889,93 +920,97 @@ k_stored_weights(int transform, double tbx, double tby, double tbz, int nmeas,
 }
 
 // The stored-row weights of one model and their fp16 split in one launch, for
-// surveys of at most kWsThreads * kWsPer stations: block n computes every
-// station's weights (k_stored_weights' arithmetic, raw-row weights written to
-// w_raw), scales them by J's row scales, takes the row's maximum and splits
-// them (k_split_rows_small's arithmetic) -- the same values as the two
-// launches, without the weights' round trip through HBM.  The stations'
-// records move through shared memory (the misfit and raw-weight records of
-// kWsThreads stations at a time, the scaled stored weights of all), so that
-// every global access is coalesced and the split runs one thread per element.
-// Rows n >= nmod are zero padding (scale 1), as in the split.
-constexpr int kWsThreads = 512;
-constexpr int kWsPer = 2;
+// surveys of at most kWsCtas * kWsThreads stations: a cluster of kWsCtas
+// CTAs per model, CTA q taking stations q * kWsThreads.. (one per thread),
+// computes every station's weights (k_stored_weights' arithmetic, raw-row
+// weights written to w_raw), scales them by J's row scales, takes the row's
+// maximum -- each CTA's through distributed shared memory -- and splits them
+// (k_split_rows_small's arithmetic): the same values as the two launches,
+// without the weights' round trip through HBM.  The stations' records move
+// through shared memory, so that every global access is coalesced and the
+// split runs one thread per element.  Rows n >= nmod are zero padding
+// (scale 1), as in the split.
+constexpr int kWsCtas = 4;
+constexpr int kWsThreads = 256;
 template <int KIND>
-constexpr int weights_split_smem() {
-  return (kWsThreads * kind_raw(KIND) + kWsThreads * kWsPer * stored_rows(KIND)) * 8;
-}
-template <int KIND>
-__global__ void __launch_bounds__(kWsThreads)
+__global__ void __cluster_dims__(kWsCtas, 1, 1) __launch_bounds__(kWsThreads)
 k_weights_split(int transform, double tbx, double tby, double tbz, int nmeas, int nmod,
                 const double *__restrict__ misfit, long long ld_misfit,
                 const double *__restrict__ rawd, MagField mf, double *__restrict__ w_raw,
                 const float *__restrict__ colscale, float *__restrict__ rowscale,
                 __half *__restrict__ hi, __half *__restrict__ lo, long long ld_dst) {
+  namespace cg = cooperative_groups;
   constexpr int kind = KIND;
   constexpr int raw = kind_raw(kind);
   constexpr int ns = stored_rows(kind);
-  extern __shared__ double ws_smem[];
-  double *rec = ws_smem;                       // [kWsThreads][raw]: misfit, then raw weights
-  double *stw = ws_smem + kWsThreads * raw;    // [nmeas][ns]: scaled stored weights
-  const int n = blockIdx.x, t = threadIdx.x;
+  __shared__ double rec[kWsThreads * raw];  // misfit, then raw-weight records
+  __shared__ double stw[kWsThreads * ns];   // scaled stored weights
+  __shared__ float red[kWsThreads / 32];
+  __shared__ float cta_max;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int q = (int)cluster.block_rank(), n = blockIdx.x / kWsCtas, t = threadIdx.x;
+  const int s0 = q * kWsThreads, count = max(0, min(kWsThreads, nmeas - s0)), s = s0 + t;
   const bool live = n < nmod;
   const bool plain = transform == TR_NONE;
   const double *mis = misfit + (long long)n * ld_misfit;
-  double *wr_row = w_raw + (long long)n * nmeas * raw;
   float mf32 = 0.0f;
-  for (int s0 = 0; s0 < nmeas; s0 += kWsThreads) {
-    const int count = min(kWsThreads, nmeas - s0), s = s0 + t;
-    if (live && plain) copy_records<raw>(rec, mis + (long long)s0 * raw, count);
-    __syncthreads();
-    if (live && t < count) {
-      double w[10], v[ns];
-      station_weights<raw>(transform, tbx, tby, tbz, rec + t * raw, plain ? 0.0 : mis[s],
-                           plain ? nullptr : rawd + (long long)n * nmeas * raw + (long long)s * raw,
-                           w);
-      if (!plain) {
+  if (live && plain) copy_records<raw>(rec, mis + (long long)s0 * raw, count);
+  __syncthreads();
+  if (live && t < count) {
+    double w[10], v[ns];
+    station_weights<raw>(transform, tbx, tby, tbz, rec + t * raw, plain ? 0.0 : mis[s],
+                         plain ? nullptr : rawd + (long long)n * nmeas * raw + (long long)s * raw,
+                         w);
+    if (!plain) {
 #pragma unroll
-        for (int c = 0; c < raw; ++c) rec[t * raw + c] = w[c];
-      }
-      stored_weights<kind>(w, mf, v);
-#pragma unroll
-      for (int q = 0; q < ns; ++q) {
-        // times J's row scale, a power of two: an exponent add
-        const double x = scale_pow2_ftz(v[q], pow2_exponent(colscale[(long long)s * ns + q]));
-        stw[s * ns + q] = x;
-        mf32 = fmaxf(mf32, fabsf(approx_f32(x)));
-      }
+      for (int c = 0; c < raw; ++c) rec[t * raw + c] = w[c];
     }
-    __syncthreads();
-    if (live) copy_records<raw>(wr_row + (long long)s0 * raw, rec, count);
-    __syncthreads();
+    stored_weights<kind>(w, mf, v);
+#pragma unroll
+    for (int k = 0; k < ns; ++k) {
+      // times J's row scale, a power of two: an exponent add
+      const double x = scale_pow2_ftz(v[k], pow2_exponent(colscale[(long long)s * ns + k]));
+      stw[t * ns + k] = x;
+      mf32 = fmaxf(mf32, fabsf(approx_f32(x)));
+    }
   }
-  __shared__ double red[kWsThreads / 32];
-  __shared__ float sh_scale;
-  const double m = warp_max_d((double)mf32);
-  if ((t & 31) == 0) red[t >> 5] = m;
-  __syncthreads();
+  // the maxima in float (the truncated values are floats; an FP64 maximum
+  // would only load the FP64 pipe)
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mf32 = fmaxf(mf32, __shfl_down_sync(0xffffffffu, mf32, o));
+  if ((t & 31) == 0) red[t >> 5] = mf32;
+  __syncthreads();  // the records and the warps' maxima are in
+  if (live) copy_records<raw>(w_raw + (long long)n * nmeas * raw + (long long)s0 * raw, rec, count);
   if (t == 0) {
-    double mm = 0.0;
-    for (int w = 0; w < kWsThreads / 32; ++w) mm = fmax(mm, red[w]);
-    sh_scale = (float)pow2_scale(mm);
-    rowscale[n] = sh_scale;
+    float mm = 0.0f;
+    for (int w = 0; w < kWsThreads / 32; ++w) mm = fmaxf(mm, red[w]);
+    cta_max = mm;
   }
+  cluster.sync();  // every CTA's maximum is in
+  float mm = 0.0f;
+  for (int r = 0; r < kWsCtas; ++r) mm = fmaxf(mm, *cluster.map_shared_rank(&cta_max, r));
+  __shared__ float sh_scale;
+  if (t == 0) sh_scale = (float)pow2_scale((double)mm);
   __syncthreads();
-  const int kinv = -pow2_exponent(sh_scale);  // dividing by the scale: an exponent add
-  __half *h = hi + (long long)n * ld_dst;
-  __half *l = lo + (long long)n * ld_dst;
-  const int nel = nmeas * ns;
-  for (int i = t; i < nel; i += kWsThreads) {
+  const float scale = sh_scale;
+  if (q == 0 && t == 0) rowscale[n] = scale;
+  const int kinv = -pow2_exponent(scale);  // dividing by the scale: an exponent add
+  __half *h = hi + (long long)n * ld_dst + (long long)s0 * ns;
+  __half *l = lo + (long long)n * ld_dst + (long long)s0 * ns;
+  for (int i = t; i < count * ns; i += kWsThreads) {
     const float x = live ? f64_to_f32_ftz(scale_pow2_ftz(stw[i], kinv)) : 0.0f;
     const __half hv = __float2half_rn(x);
     h[i] = hv;
     l[i] = __float2half_rn(__fsub_rn(x, __half2float(hv)));
   }
-  // padding columns
-  for (long long c = (long long)nel + t; c < ld_dst; c += kWsThreads) {
-    h[c] = __float2half_rn(0.0f);
-    l[c] = __float2half_rn(0.0f);
+  if (q == kWsCtas - 1) {  // padding columns
+    __half *hr = hi + (long long)n * ld_dst, *lr = lo + (long long)n * ld_dst;
+    for (long long c = (long long)nmeas * ns + t; c < ld_dst; c += kWsThreads) {
+      hr[c] = __float2half_rn(0.0f);
+      lr[c] = __float2half_rn(0.0f);
+    }
   }
+  cluster.sync();  // no CTA leaves while another may read its maximum
 }
 
 // grads[n][ngrid + j] = 2 sum_s sum_r w_raw[n][s][r] bgsens[s][r][j]; block (j, n)
@@ -1179,7 +1214,7 @@ cudaError_t launch_stored_weights(int kind, int transform, double tbx, double tb
 }
 
 bool weights_split_fits(int nmeas, long long ld_dst, int nrow_pad) {
-  return nmeas <= kWsThreads * kWsPer && ld_dst <= kSmallRow && nrow_pad >= 1;
+  return nmeas <= kWsThreads * kWsCtas && ld_dst <= kSmallRow && nrow_pad >= 1;
 }
 
 cudaError_t launch_weights_split(int kind, int transform, double tbx, double tby, double tbz,
@@ -1190,14 +1225,9 @@ cudaError_t launch_weights_split(int kind, int transform, double tbx, double tby
   if (!weights_split_fits(nmeas, ld_dst, nrow_pad)) return cudaErrorInvalidValue;
   if ((long long)nmeas * stored_rows(kind) > ld_dst) return cudaErrorInvalidValue;
 #define J3G_WS(K)                                                                             \
-  do {                                                                                        \
-    const cudaError_t ea = allow_smem_once(reinterpret_cast<const void *>(k_weights_split<K>),    \
-                                              weights_split_smem<K>());                       \
-    if (ea != cudaSuccess) return ea;                                                         \
-    k_weights_split<K><<<nrow_pad, kWsThreads, weights_split_smem<K>(), st>>>(                \
-        transform, tbx, tby, tbz, nmeas, nmod, misfit, ld_misfit, rawd, mf, w_raw, colscale,   \
-        rowscale, static_cast<__half *>(hi), static_cast<__half *>(lo), ld_dst);               \
-  } while (0)
+  k_weights_split<K><<<nrow_pad * kWsCtas, kWsThreads, 0, st>>>(                              \
+      transform, tbx, tby, tbz, nmeas, nmod, misfit, ld_misfit, rawd, mf, w_raw, colscale,     \
+      rowscale, static_cast<__half *>(hi), static_cast<__half *>(lo), ld_dst)
   switch (kind) {
     case KIND_SCALAR: J3G_WS(KIND_SCALAR); break;
     case KIND_TENSOR: J3G_WS(KIND_TENSOR); break;

@@ -80,7 +80,7 @@ cudaError_t launch_stored_weights(int kind, int transform, double tbx, double tb
                                   double *w_st, long long ld_w, cudaStream_t st);
 // The weights of launch_stored_weights and their split (launch_split_matrix
 // without centring, colscale = J's row scales) in one launch, for surveys
-// that fit one block per model (weights_split_fits): w_raw as
+// that fit one cluster of CTAs per model (weights_split_fits): w_raw as
 // launch_stored_weights writes it, hi / lo / rowscale as the split does.
 bool weights_split_fits(int nmeas, long long ld_dst, int nrow_pad);
 cudaError_t launch_weights_split(int kind, int transform, double tbx, double tby, double tbz,
