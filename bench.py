@@ -195,10 +195,11 @@ def max_over_ranks(v, world):
 #   ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum
 #       --clock-control none --csv python bench.py --case batched --steps 2
 # (forward 3934.5 + 219.2 MB, adjoint 3813.1 + 257.6 MB).
-GEMM_DRAM_BYTES_PER_LAUNCH = 0.5 * ((3934.5 + 219.2) + (3813.1 + 257.6)) * 1e6
+GEMM_DRAM_BYTES_PER_LAUNCH = 0.5 * ((3940.2 + 117.7) + (3809.6 + 119.6)) * 1e6
 GEMM_TRAFFIC_SOURCE = ("ncu one-pass dram__bytes_read.sum + dram__bytes_write.sum of the "
-                       "full-size launches (mean of forward and adjoint) of "
-                       "`python bench.py --case batched --steps 2`, not measured in this run")
+                       "full-size launches (mean of forward and adjoint, fixed-rule plans of "
+                       "17 and 1 K splits) of `python bench.py --case batched --steps 2`, not "
+                       "measured in this run")
 
 
 def sigma_vector(s):
