@@ -379,26 +379,32 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_split_models(
       }
     }
   }
+  // the split's exponent from the binade of its largest |d|: in float, m in
+  // [2^(E-1), 2^E) with E = biased exponent - 126 (rounding to float can lift
+  // a maximum just below 2^E to 2^E, which only raises E); in FP64 (values
+  // beyond the float range), E = biased exponent - 1022
   const bool fp64 = __syncthreads_or(bad) != 0;
-  if (fp64) {
-    mf = 0.0f;
+  int el;
+  if (!fp64) {
+    const uint32_t be = (__float_as_uint(mf) >> 23) & 0xffu;
+    el = be ? (int)be - 126 - 14 : INT_MIN / 2;
+  } else {
+    el = INT_MIN / 2;
     for (long long c = c0 + threadIdx.x; c < c1; c += NT)
-      if (in_row(c)) mf = fmaxf(mf, fabsf(f64_to_f32_ftz(row[c] - cr)));
+      if (in_row(c)) {
+        const int be = (int)(((unsigned long long)__double_as_longlong(row[c] - cr) >> 52) & 0x7ff);
+        if (be) el = max(el, be - 1022 - 14);
+      }
   }
-  __shared__ float red[NT / 32];
+  __shared__ int red[NT / 32];
   __shared__ int sh_e;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mf = fmaxf(mf, __shfl_down_sync(0xffffffffu, mf, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mf;
+  el = __reduce_max_sync(0xffffffffu, el);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = el;
   __syncthreads();
   if (threadIdx.x == 0) {
-    float m = 0.0f;
-    for (int w = 0; w < NT / 32; ++w) m = fmaxf(m, red[w]);
-    // m in [2^(E-1), 2^E) with E = biased exponent - 126; rounding to float
-    // can lift a maximum just below 2^E to 2^E, which only raises E
-    const uint32_t be = (__float_as_uint(m) >> 23) & 0xffu;
-    const int el = be ? (int)be - 126 - 14 : INT_MIN / 2;
-    int e = max(row_ok ? eref[r] : 0, el);
+    int m = INT_MIN / 2;
+    for (int w = 0; w < NT / 32; ++w) m = max(m, red[w]);
+    int e = max(row_ok ? eref[r] : INT_MIN / 2, m);
     if (e == INT_MIN / 2) e = 0;  // all zero
     sh_e = e;
     sexp[r * nsp + blockIdx.x] = e;
@@ -654,14 +660,15 @@ __global__ void __launch_bounds__(kT) k_splitk_reduce4(
   const int nq = nrow / 4;
   const int n = blockIdx.y;
   // per-split scales 2^sexp[n][s]: each split's partials are brought to the
-  // smallest of them in FP32 (exact: an exponent add; most splits of a model
+  // largest of them in FP32 (an exponent add, exact but for contributions
+  // below 2^-126 of that scale, which flush to zero; most splits of a model
   // share one scale and skip it) and that one is applied with the other
   // scales at the end
   const int *se = sexp ? sexp + (long long)n * nsplit : nullptr;
   int ebase = 0;
   if (se) {
     ebase = se[0];
-    for (int s = 1; s < nsplit; ++s) ebase = min(ebase, se[s]);
+    for (int s = 1; s < nsplit; ++s) ebase = max(ebase, se[s]);
   }
   const int q0 = blockIdx.x * (kT * G) + threadIdx.x;
   const long long s4 = slice / 4;
@@ -707,12 +714,19 @@ __global__ void __launch_bounds__(kT) k_splitk_reduce4(
             for (int i = 0; i < 4; ++i) x[i] = scale_f32_ftz(x[i], k);
           }
         }
+        if (nsplit == 1) {
+          // one split: the two-sum onto zero is x + 0 (a zero's sign made
+          // positive) with no error term, bit for bit
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          float sres, err;
-          two_sum(hi[g][i], x[i], sres, err);
-          hi[g][i] = sres;
-          lo[g][i] = __fadd_rn(lo[g][i], err);
+          for (int i = 0; i < 4; ++i) hi[g][i] = __fadd_rn(x[i], 0.0f);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            float sres, err;
+            two_sum(hi[g][i], x[i], sres, err);
+            hi[g][i] = sres;
+            lo[g][i] = __fadd_rn(lo[g][i], err);
+          }
         }
       }
     if (kAhead) {

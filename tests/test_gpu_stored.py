@@ -281,25 +281,29 @@ def test_models_with_uneven_magnitudes(ctx, oracle_lib):
     """Models whose K splits differ in magnitude by many binades (a near-zero
     region, a large uniform part, one cell far above the rest): each split
     takes its own scale where the row's sampled one does not bound it, and
-    the split sums bring them together exactly."""
+    the split sums bring them together exactly.  A value beyond the float
+    range takes the split's FP64 form; a NaN reaches every datum."""
     s = small_survey(W.JOINT, seed=311, nx=24, ny=20, nz=10, nmeas=20)
     W.setup_context(ctx, s)
     ctx.build_sensitivity(capi.STORE_F16X2)
     rng = np.random.default_rng(32)
     ng = s.ngrid
-    models = np.tile(s.model, (6, 1))
+    models = np.tile(s.model, (8, 1))
     models[0, :ng // 2] *= 1e-9                       # half the cells near zero
     models[1, :ng] += 1e6                             # a large uniform part
     models[2, 40] = 1e7                               # one outlier cell, not sampled
     models[3, :ng] = rng.normal(size=ng) * np.logspace(-6, 6, ng)
     models[4, :ng] = -models[4, :ng]
     models[5, :ng] = 0.0                              # background only
-    mis = rng.normal(size=(6, s.stations.shape[0] * 10))
+    models[6, 40] = 1e39                              # beyond the float range: FP64 split
+    models[7, 40] = np.nan                            # propagates to every datum
+    mis = rng.normal(size=(8, s.stations.shape[0] * 10))
     d = ctx.batched_forward(models)
     g = ctx.batched_lqderivative(models, mis)
-    for i in range(6):
+    for i in range(7):
         check_groups(s, d[i], oracle_forward(oracle_lib, s, models[i]))
         assert relerr(g[i], oracle_lqderivative(oracle_lib, s, mis[i], models[i])) <= TOL
+    assert np.isnan(d[7]).all()
 
 
 def test_batched_adjoint_long_residual_rows(ctx, oracle_lib):
