@@ -328,57 +328,72 @@ __device__ __forceinline__ float centred_f32(double v, float ch, float cl, bool 
   return __fadd_rn(__fsub_rn(vh, ch), __fsub_rn(vl, cl));
 }
 
-// One block per (model row, K split): d = v - centre in float arithmetic
-// (centred_f32) kept in registers; the split's exponent e = max(eref[row],
-// frexp exponent of max |d| - 14) (sexp[row][split]), so |d| / 2^e < 2^14;
-// then hi + lo of d / 2^e (a float multiply by a power of two, exact).  A
-// split with a value beyond the float range, an exponent outside
-// [-100, 100], or more columns than kT * kSplitPer (plans pinned past the
-// accuracy bound, WIDE) is computed in FP64 instead: d = v - centre, then
-// one rounding of d / 2^e to float.  NT threads a block: 256 for splits of up
-// to 4096 columns, 512 up to 8192.
-constexpr int kSplitPer = 16;
-template <bool WIDE, int NT>
-__global__ void __launch_bounds__(NT, 1024 / NT) k_split_models(
+// One block per (model row, K split), streaming: d = v - centre in float
+// arithmetic (centred_f32), split at once with the row's sampled exponent
+// e0 = eref[row] into hi + lo of d / 2^e0 (a float multiply by a power of
+// two, exact), while the block takes max |d|.  The split's exponent is
+// e = max(e0, frexp exponent of max |d| - 14) (sexp[row][split]), so
+// |d| / 2^e < 2^14; where it is not e0 -- values above the row's sample --
+// the block splits its columns again with e (a second read, from L2).  A
+// split with a value beyond the float range or an exponent outside
+// [-100, 100] is split again in FP64: d = v - centre, then one rounding of
+// d / 2^e to float.  Each thread takes column pairs, kSplitBatch of them per
+// batch of loads.
+constexpr int kSplitThreads = 256;
+constexpr int kSplitBatch = 4;
+__global__ void __launch_bounds__(kSplitThreads) k_split_models(
     const double *__restrict__ src, long long ld_src, int nrow, long long ncol,
     const double *__restrict__ centre, const int *__restrict__ eref, __half *__restrict__ hi,
     __half *__restrict__ lo, long long ld_dst, long long cols_per_split, int nsp,
     int *__restrict__ sexp) {
+  constexpr int NT = kSplitThreads;
   const long long r = blockIdx.y;
   const long long c0 = (long long)blockIdx.x * cols_per_split;
   const long long c1 = min(ld_dst, c0 + cols_per_split);
   const bool row_ok = r < nrow;
   const double cr = row_ok ? centre[r] : 0.0;
-  const double *row = src + r * ld_src;
-  auto in_row = [&](long long c) { return row_ok && c < c1 && c < ncol; };
-  float x[kSplitPer];
-  float mf = 0.0f;
-  bool bad = WIDE;
-  // in registers, each thread holds column pairs (c, c + 1), c = c0 + 2 (t + u NT):
-  // x[2u], x[2u + 1] (c0 and the split ends are multiples of 64, so a pair
-  // never straddles them)
-  if constexpr (!WIDE) {
-    const float ch = f64_to_f32_ftz(cr), cl = f64_to_f32_ftz(cr - (double)ch);
-    // columns of this thread relative to c0, and the end of the row's values
-    const int j0 = 2 * (int)threadIdx.x;
-    const int jend = row_ok ? (int)(min(c1, ncol) - c0) : 0;
-    const double *rp = row + c0;
+  const int er = row_ok ? eref[r] : INT_MIN / 2;
+  const int e0 = er == INT_MIN / 2 ? 0 : er;  // the provisional exponent
+  const float ch = f64_to_f32_ftz(cr), cl = f64_to_f32_ftz(cr - (double)ch);
+  // columns relative to c0: this split's (jn, even) and the row's values in it
+  const int jn = (int)(c1 - c0);
+  const int jend = row_ok ? (int)max(0LL, min(c1, ncol) - c0) : 0;
+  const double *rp = src + r * ld_src + c0;
+  __half2 *hp = reinterpret_cast<__half2 *>(hi + r * ld_dst + c0);
+  __half2 *lp = reinterpret_cast<__half2 *>(lo + r * ld_dst + c0);
+  auto put = [&](int p, float x0, float x1) {  // column pair 2p, 2p + 1
+    const __half2 hv = __floats2half2_rn(x0, x1);
+    const float2 hf = __half22float2(hv);
+    hp[p] = hv;
+    lp[p] = __floats2half2_rn(__fsub_rn(x0, hf.x), __fsub_rn(x1, hf.y));
+  };
+  // float pass at a given exponent: split and store every pair, return max |d|
+  auto float_pass = [&](int ex, bool &bad) {
+    const float inv = __uint_as_float((uint32_t)(127 - ex) << 23);  // 2^-ex
+    float m = 0.0f;
+    for (int p0 = (int)threadIdx.x; 2 * p0 < jn; p0 += NT * kSplitBatch) {
+      double v[2 * kSplitBatch];  // a batch of loads in flight
 #pragma unroll
-    for (int h0 = 0; h0 < kSplitPer; h0 += 8) {
-      double v[8];  // a batch of loads in flight
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int j = j0 + ((h0 + u) >> 1) * 2 * NT + (u & 1);
+      for (int u = 0; u < 2 * kSplitBatch; ++u) {
+        const int j = 2 * (p0 + (u >> 1) * NT) + (u & 1);
         v[u] = j < jend ? rp[j] : 0.0;
       }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int j = j0 + ((h0 + u) >> 1) * 2 * NT + (u & 1);
-        x[h0 + u] = j < jend ? centred_f32(v[u], ch, cl, bad) : 0.0f;
-        mf = fmaxf(mf, fabsf(x[h0 + u]));
+      for (int k = 0; k < kSplitBatch; ++k) {
+        const int p = p0 + k * NT;
+        if (2 * p >= jn) break;
+        const float x0 = 2 * p < jend ? centred_f32(v[2 * k], ch, cl, bad) : 0.0f;
+        const float x1 = 2 * p + 1 < jend ? centred_f32(v[2 * k + 1], ch, cl, bad) : 0.0f;
+        m = fmaxf(m, fmaxf(fabsf(x0), fabsf(x1)));
+        put(p, x0 * inv, x1 * inv);
       }
     }
-  }
+    return m;
+  };
+  const bool fast0 = e0 >= -100 && e0 <= 100;
+  bool bad = !fast0;
+  float mf = 0.0f;
+  if (fast0) mf = float_pass(e0, bad);
   // the split's exponent from the binade of its largest |d|: in float, m in
   // [2^(E-1), 2^E) with E = biased exponent - 126 (rounding to float can lift
   // a maximum just below 2^E to 2^E, which only raises E); in FP64 (values
@@ -390,11 +405,10 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_split_models(
     el = be ? (int)be - 126 - 14 : INT_MIN / 2;
   } else {
     el = INT_MIN / 2;
-    for (long long c = c0 + threadIdx.x; c < c1; c += NT)
-      if (in_row(c)) {
-        const int be = (int)(((unsigned long long)__double_as_longlong(row[c] - cr) >> 52) & 0x7ff);
-        if (be) el = max(el, be - 1022 - 14);
-      }
+    for (int j = (int)threadIdx.x; j < jend; j += NT) {
+      const int be = (int)(((unsigned long long)__double_as_longlong(rp[j] - cr) >> 52) & 0x7ff);
+      if (be) el = max(el, be - 1022 - 14);
+    }
   }
   __shared__ int red[NT / 32];
   __shared__ int sh_e;
@@ -404,40 +418,26 @@ __global__ void __launch_bounds__(NT, 1024 / NT) k_split_models(
   if (threadIdx.x == 0) {
     int m = INT_MIN / 2;
     for (int w = 0; w < NT / 32; ++w) m = max(m, red[w]);
-    int e = max(row_ok ? eref[r] : INT_MIN / 2, m);
+    int e = max(er, m);
     if (e == INT_MIN / 2) e = 0;  // all zero
     sh_e = e;
     sexp[r * nsp + blockIdx.x] = e;
   }
   __syncthreads();
   const int e = sh_e;
-  auto put = [&](long long c, float xs) {
-    const __half hv = __float2half_rn(xs);
-    hi[r * ld_dst + c] = hv;
-    lo[r * ld_dst + c] = __float2half_rn(__fsub_rn(xs, __half2float(hv)));
-  };
+  if (!fp64 && e == e0) return;  // the first pass stands
   if (!fp64 && e >= -100 && e <= 100) {
-    const float inv = __uint_as_float((uint32_t)(127 - e) << 23);  // 2^-e
-    const int jn = (int)(c1 - c0);
-    __half2 *hp = reinterpret_cast<__half2 *>(hi + r * ld_dst + c0);
-    __half2 *lp = reinterpret_cast<__half2 *>(lo + r * ld_dst + c0);
-#pragma unroll
-    for (int u = 0; u < kSplitPer; u += 2) {
-      const int p = (int)threadIdx.x + (u >> 1) * NT;  // column pair 2p, 2p + 1
-      if (2 * p < jn) {  // one 4-byte store per part
-        const float x0 = x[u] * inv, x1 = x[u + 1] * inv;
-        const __half2 hv = __floats2half2_rn(x0, x1);
-        const float2 hf = __half22float2(hv);
-        hp[p] = hv;
-        lp[p] = __floats2half2_rn(__fsub_rn(x0, hf.x), __fsub_rn(x1, hf.y));
-      }
-    }
+    bool unused = false;
+    float_pass(e, unused);
   } else {
     // 2^-e as a double (split exponents of finite doubles stay within
     // -1100 .. 1040; beyond the normal range the scaling saturates)
     const double inv64 = __longlong_as_double((long long)min(2046, max(1, 1023 - e)) << 52);
-    for (long long c = c0 + threadIdx.x; c < c1; c += NT)
-      put(c, in_row(c) ? f64_to_f32_ftz((row[c] - cr) * inv64) : 0.0f);
+    for (int p = (int)threadIdx.x; 2 * p < jn; p += NT) {
+      const float x0 = 2 * p < jend ? f64_to_f32_ftz((rp[2 * p] - cr) * inv64) : 0.0f;
+      const float x1 = 2 * p + 1 < jend ? f64_to_f32_ftz((rp[2 * p + 1] - cr) * inv64) : 0.0f;
+      put(p, x0, x1);
+    }
   }
 }
 
@@ -1112,15 +1112,8 @@ cudaError_t launch_split_models(const double *src, long long ld_src, int nrow, l
   if (e != cudaSuccess) return e;
   dim3 grid(nsp, nrow_pad);
   __half *h = static_cast<__half *>(hi), *l = static_cast<__half *>(lo);
-  if (cols_per_split <= 256LL * kSplitPer)
-    k_split_models<false, 256><<<grid, 256, 0, st>>>(src, ld_src, nrow, ncol, centre, eref, h, l,
-                                                     ld_dst, cols_per_split, nsp, sexp);
-  else if (cols_per_split <= 512LL * kSplitPer)
-    k_split_models<false, 512><<<grid, 512, 0, st>>>(src, ld_src, nrow, ncol, centre, eref, h, l,
-                                                     ld_dst, cols_per_split, nsp, sexp);
-  else
-    k_split_models<true, 512><<<grid, 512, 0, st>>>(src, ld_src, nrow, ncol, centre, eref, h, l,
-                                                    ld_dst, cols_per_split, nsp, sexp);
+  k_split_models<<<grid, kSplitThreads, 0, st>>>(src, ld_src, nrow, ncol, centre, eref, h, l,
+                                                  ld_dst, cols_per_split, nsp, sexp);
   return cudaGetLastError();
 }
 
