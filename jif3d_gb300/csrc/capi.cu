@@ -776,12 +776,14 @@ cudaError_t product_launches(j3g_context *c, int dir, const GemmOperands &g, int
 // the SMs, and one-SM 128-wide tiles where the pair kernel would run -- once
 // after an untimed run (CUDA events on the context's stream), keeps the
 // fastest for the context's lifetime and reuses it.  A candidate is timed
-// as `run` queues it (nsplit, tile): the product with its split sums, and for
-// the forward the models' split, which follows the product's K splits.
+// as `run` queues it (operands, nsplit, tile): the product with its split
+// sums, and for the forward the models' split, which follows the product's K
+// splits.
 // Every candidate keeps at most kMaxKbPerSplit k-blocks per split, the bound
 // that holds the FP32 register sums to their accuracy.
 int gemm_plan(j3g_context *c, int dir, const GemmOperands &g, long long slice,
-              const std::function<cudaError_t(int, int)> &run, j3g_context::GemmPlan &plan) {
+              const std::function<cudaError_t(const GemmOperands &, int, int)> &run,
+              j3g_context::GemmPlan &plan) {
   const int tile0 = gemm_n_tile((int)g.n);
   plan.tile = tile0;
   plan.nsplit = choose_splits(g.m, (int)(g.n_pad / tile0), g.ld);
@@ -842,9 +844,9 @@ int gemm_plan(j3g_context *c, int dir, const GemmOperands &g, long long slice,
   float best = 0.0f;
   for (auto &p : cand) {
     float ms = 0.0f;
-    cudaError_t e = run(p.second, p.first);
+    cudaError_t e = run(gt, p.second, p.first);
     if (e == cudaSuccess) e = cudaEventRecord(a, c->stream);
-    if (e == cudaSuccess) e = run(p.second, p.first);
+    if (e == cudaSuccess) e = run(gt, p.second, p.first);
     if (e == cudaSuccess) e = cudaEventRecord(b, c->stream);
     if (e == cudaSuccess) e = cudaEventSynchronize(b);
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
@@ -913,7 +915,7 @@ int batched_forward_pass(j3g_context *c, int nmod, const double *d_models, doubl
     // (J 1) is added back in FP64 after the product, so a large uniform part
     // of a model -- whose tensor response is nearly zero -- does not eat into
     // the FP32 accuracy) and split with one scale per K split of the product
-    auto run = [&](int nsplit, int tile) -> cudaError_t {
+    auto run = [&](const GemmOperands &go, int nsplit, int tile) -> cudaError_t {
       const int nsp = gemm_splits_used(ldK, nsplit);
       cudaError_t e;
       {
@@ -924,12 +926,12 @@ int batched_forward_pass(j3g_context *c, int nmod, const double *d_models, doubl
       }
       if (e != cudaSuccess) return e;
       c->launches += 2;
-      return product_launches(c, 0, g, nsplit, tile, R, slice, ss);
+      return product_launches(c, 0, go, nsplit, tile, R, slice, ss);
     };
     j3g_context::GemmPlan plan;
     J3G_TRY(gemm_plan(c, 0, g, slice, run, plan));
     c->last_plan[0] = plan;
-    const cudaError_t e = run(plan.nsplit, plan.tile);
+    const cudaError_t e = run(g, plan.nsplit, plan.tile);
     if (e != cudaSuccess) return cuda_fail(c, e, "forward product");
   }
   TimedScope ts(c, J3G_TIMER_EPILOGUE);
@@ -1015,8 +1017,8 @@ int batched_adjoint_pass(j3g_context *c, int nmod, const double *d_models,
     ss.ld_out = np;
     ss.modscale = ptr<float>(c->mscale);
     ss.factor = 2.0;
-    auto run = [&](int nsplit, int tile) {
-      return product_launches(c, 1, g, nsplit, tile, K, slice, ss);
+    auto run = [&](const GemmOperands &go, int nsplit, int tile) {
+      return product_launches(c, 1, go, nsplit, tile, K, slice, ss);
     };
     j3g_context::GemmPlan plan;
     J3G_TRY(gemm_plan(c, 1, g, slice, run, plan));

@@ -765,6 +765,22 @@ bool make_tiled_map(CUtensorMap *map, const void *base, long long rows, long lon
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// Dynamic shared-memory opt-in of a kernel, once per kernel and device: the
+// launchers stay free of non-stream CUDA calls after the first launch, so a
+// caller can capture later launches in a CUDA graph.
+cudaError_t allow_smem_once(const void *kernel, int bytes) {
+  static std::mutex mu;
+  static std::set<std::pair<const void *, int>> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count({kernel, dev})) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) done.insert({kernel, dev});
+  return e;
+}
+
 template <int BN, bool F16>
 cudaError_t launch_bn(const GemmOperands &g, int nsplit, float *P, long long ldp, long long slice,
                       int *err, cudaStream_t st) {
@@ -811,22 +827,6 @@ cudaError_t launch_pair(const GemmOperands &g, int nsplit, float *P, long long l
 }
 
 }  // namespace
-
-// Dynamic shared-memory opt-in of a kernel, once per kernel and device: the
-// launchers stay free of non-stream CUDA calls after the first launch, so a
-// caller can capture later launches in a CUDA graph.
-cudaError_t allow_smem_once(const void *kernel, int bytes) {
-  static std::mutex mu;
-  static std::set<std::pair<const void *, int>> done;
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  std::lock_guard<std::mutex> lock(mu);
-  if (done.count({kernel, dev})) return cudaSuccess;
-  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e == cudaSuccess) done.insert({kernel, dev});
-  return e;
-}
 
 // N tile of the batched products: 64 or 128 on one SM, 256 on a CTA pair.
 int gemm_n_tile(int n) { return n <= 64 ? 64 : (n <= 128 ? 128 : kPairN); }

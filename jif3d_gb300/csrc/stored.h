@@ -107,9 +107,6 @@ struct GemmOperands {
   // expires (after 20 ms) and the launch reports an error code (j3g_set_test_fault)
   int fault = 0;
 };
-// Dynamic shared-memory opt-in of a kernel (cudaFuncSetAttribute), made
-// once per kernel and device so that later launches stay capturable.
-cudaError_t allow_smem_once(const void *kernel, int bytes);
 int gemm_n_tile(int n);
 int gemm_splits_used(long long ld, int nsplit);
 // k-blocks (64 columns) per K split: split s covers k-blocks [s kb, (s + 1) kb).
