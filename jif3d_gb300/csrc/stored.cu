@@ -241,8 +241,8 @@ __global__ void k_split_chunks(const double *__restrict__ src, long long ld_src,
 // values.  The power-of-two scale only sets the fp16 exponent range (hi and
 // lo keep 11 bits each at any scale that keeps them normal), so a row scale
 // taken from the same sample serves every K split of the product whose
-// values it bounds; a split with larger values takes its own, larger scale,
-// known before its split because one block holds the split's columns.  The
+// values it bounds; a split with larger values takes its own, larger scale
+// (its block splits the columns again once it has their maximum).  The
 // split-sum kernel applies each split's scale (sexp) to its partial sums.
 constexpr int kCentreRuns = 64;    // contiguous runs sampled per model row
 constexpr int kCentreRun = 32;     // values per run

@@ -62,6 +62,8 @@ cudaError_t launch_splitk_reduce(const float *P, int nsplit, long long slice, in
 // pass: centre[r] an estimate of row r's mean (removed before the split), and
 // per split the power-of-two scale 2^sexp[r][s]: row r = centre[r] + the
 // split's 2^sexp * (hi + lo) on its columns.  Rows beyond nrow are zero.
+// sexp holds nrow_pad * (nsp + 1) ints: the table, then the rows' sampled
+// exponents.
 cudaError_t launch_split_models(const double *src, long long ld_src, int nrow, long long ncol,
                                 void *hi, void *lo, long long ld_dst, int nrow_pad,
                                 long long cols_per_split, int nsp, double *centre, int *sexp,
