@@ -968,6 +968,11 @@ k_weights_split(int transform, double tbx, double tby, double tbz, int nmeas, in
   const bool plain = transform == TR_NONE;
   const double *mis = misfit + (long long)n * ld_misfit;
   float mf32 = 0.0f;
+  // J's row scales of this station (as exponents), loaded with the records
+  int cexp[ns];
+#pragma unroll
+  for (int k = 0; k < ns; ++k)
+    cexp[k] = (live && t < count) ? pow2_exponent(colscale[(long long)s * ns + k]) : 0;
   if (live && plain) copy_records<raw>(rec, mis + (long long)s0 * raw, count);
   __syncthreads();
   if (live && t < count) {
@@ -983,7 +988,7 @@ k_weights_split(int transform, double tbx, double tby, double tbz, int nmeas, in
 #pragma unroll
     for (int k = 0; k < ns; ++k) {
       // times J's row scale, a power of two: an exponent add
-      const double x = scale_pow2_ftz(v[k], pow2_exponent(colscale[(long long)s * ns + k]));
+      const double x = scale_pow2_ftz(v[k], cexp[k]);
       stw[t * ns + k] = x;
       mf32 = fmaxf(mf32, fabsf(approx_f32(x)));
     }
