@@ -541,6 +541,8 @@ def run_batched(args, rank, world, local):
     rng = np.random.default_rng(44)
     d_obs += torch.tensor(sig * rng.normal(size=n * 10), dtype=torch.float64, device=dev)
     w = torch.tensor(1.0 / sig ** 2, dtype=torch.float64, device=dev)
+    # the weighted misfit (d - d_obs) w as one elementwise pass: d w - d_obs w
+    neg_obs_w = -(d_obs * w)
 
     # sensitivity build (once per geometry, outside the timed steps)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -560,7 +562,7 @@ def run_batched(args, rank, world, local):
 
     def step():
         ctx.batched_forward_device(nmod, models.data_ptr(), data.data_ptr())
-        torch.mul(torch.sub(data, d_obs, out=misfit), w, out=misfit)
+        torch.addcmul(neg_obs_w, data, w, out=misfit)
         ctx.batched_lqderivative_device(nmod, models.data_ptr(), misfit.data_ptr(),
                                         grads.data_ptr())
 
@@ -662,10 +664,10 @@ def run_batched(args, rank, world, local):
                                                  ("mis", data.shape), ("grads", s.models.shape))}
         st["models"].copy_(torch.from_numpy(s.models))
         sets.append(st)
-    obs_t, w_t = d_obs.cpu(), torch.from_numpy(1.0 / sig ** 2)
+    neg_obs_w_t, w_t = neg_obs_w.cpu(), torch.from_numpy(1.0 / sig ** 2)
 
     def host_misfit(st):
-        torch.mul(torch.sub(st["data"], obs_t, out=st["mis"]), w_t, out=st["mis"])
+        torch.addcmul(neg_obs_w_t, st["data"], w_t, out=st["mis"])
 
     def e2e_blocking(nsteps):
         st = sets[0]
@@ -772,7 +774,7 @@ def run_batched(args, rank, world, local):
         "sensitivity_build_ms": build_ms, "sensitivity_bytes": info["bytes"],
         "gpu_launches": launches, "clocks": clk,
         "step": "one CUDA graph per step (batched forward, weighted misfit, batched "
-                "adjoint: %d library kernels + 2 torch kernels), replayed" % launches_per_step,
+                "adjoint: %d library kernels + 1 torch kernel), replayed" % launches_per_step,
         "ms_per_step_by_phase": phase_ms,
         "plain_fp64": {"value": plain_value, "unit": UNIT, "ms_per_step": plain_ms,
                        "what": "FP64 matrix-free fwd+adjoint of one model, same survey"},
