@@ -255,10 +255,10 @@ def test_pinned_gemm_plans(ctx, oracle_lib):
         ctx.set_gemm_plan(0, 4, 96)
 
 
-def test_models_split_wider_than_a_block(ctx, oracle_lib):
-    """A plan pinned to one K split over more columns than one block of the
-    models' split holds in registers (4320 cells, 68 k-blocks): the split
-    takes its two-pass form and the products still match the oracle."""
+def test_models_split_over_pinned_splits(ctx, oracle_lib):
+    """Plans pinned to one K split (4320 cells, 68 k-blocks in one block of
+    the models' split) and to three: each split's scale and the split sums
+    follow the plan, and the products match the oracle."""
     s = small_survey(W.JOINT, seed=310, nx=20, ny=18, nz=12, nmeas=24)
     W.setup_context(ctx, s)
     ctx.build_sensitivity(capi.STORE_F16X2)
