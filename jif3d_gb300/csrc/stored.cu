@@ -667,8 +667,11 @@ __global__ void __launch_bounds__(kT) k_splitk_reduce4(
   const int *se = sexp ? sexp + (long long)n * nsplit : nullptr;
   int ebase = 0;
   if (se) {
-    ebase = se[0];
-    for (int s = 1; s < nsplit; ++s) ebase = max(ebase, se[s]);
+    // one load per lane and a warp maximum (every thread of the block gets
+    // here): a loop over the splits in each thread was a chain of round trips
+    int e = INT_MIN;
+    for (int s = threadIdx.x & 31; s < nsplit; s += 32) e = max(e, se[s]);
+    ebase = __reduce_max_sync(0xffffffffu, e);
   }
   const int q0 = blockIdx.x * (kT * G) + threadIdx.x;
   const long long s4 = slice / 4;
