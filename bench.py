@@ -659,7 +659,7 @@ def run_batched(args, rank, world, local):
     def pinned(shape):
         return torch.empty(shape, dtype=torch.float64, pin_memory=True)
     sets = []
-    for _ in range(2):  # host buffers of two steps in flight
+    for _ in range(3):  # host buffers of three steps in flight
         st = {k: pinned(shape) for k, shape in (("models", s.models.shape), ("data", data.shape),
                                                  ("mis", data.shape), ("grads", s.models.shape))}
         st["models"].copy_(torch.from_numpy(s.models))
@@ -680,27 +680,31 @@ def run_batched(args, rank, world, local):
     def e2e_pipelined(nsteps):
         """Step i waits for its own data, forms the misfit, queues its
         derivative and then the forward of step i + 2 (the batches' models are
-        known ahead, as for independent batches); the gradient of step i - 1
-        is taken (waited for) last.  The forward's 268 MB model copy so gets
-        two products of lead time, and at most four calls are in flight."""
+        known ahead, as for independent batches); the gradient of step i - 2
+        is taken (waited for) last, before its host buffers come round again
+        (three sets).  Waiting for the gradient of step i - 1 there instead
+        held the host until that gradient (268 MB) had come back, so the
+        forward of step i + 3 was queued late and waited for its models.  At
+        most four calls are in flight."""
         fwd, adj = {}, {}
 
         def queue_fwd(i):
-            st = sets[i % 2]
+            st = sets[i % 3]
             fwd[i] = ctx.batched_forward_async(st["models"].numpy(), out=st["data"].numpy())
         for i in range(min(2, nsteps)):
             queue_fwd(i)
         for i in range(nsteps):
-            st = sets[i % 2]
+            st = sets[i % 3]
             ctx.batched_wait(fwd[i])
             host_misfit(st)
             adj[i] = ctx.batched_lqderivative_async(st["models"].numpy(), st["mis"].numpy(),
                                                     out=st["grads"].numpy())
             if i + 2 < nsteps:
                 queue_fwd(i + 2)
-            if i >= 1:
-                ctx.batched_wait(adj[i - 1])
-        ctx.batched_wait(adj[nsteps - 1])
+            if i >= 2:
+                ctx.batched_wait(adj[i - 2])
+        for i in range(max(0, nsteps - 2), nsteps):
+            ctx.batched_wait(adj[i])
 
     e2e_pipelined(2)
     e2e_blocking(2)
@@ -721,12 +725,21 @@ def run_batched(args, rank, world, local):
     link["bound_ms_per_step"] = (nbytes_in + nbytes_out) / (link["both_gbs"] * 1e6)
     link["bound_under_load_ms_per_step"] = ((nbytes_in + nbytes_out) /
                                             (link["both_under_load_gbs"] * 1e6))
+    # the host's misfit alone (it sits between the two calls of a step)
+    mis_t = []
+    for _ in range(7):
+        a0 = time.perf_counter()
+        host_misfit(sets[0])
+        mis_t.append((time.perf_counter() - a0) * 1e3)
     e2e = {"value": units * world * args.steps / e2e_s / 1e6, "unit": UNIT,
            "h2d_bytes_per_step": nbytes_in, "host_buffers": "pinned",
            "d2h_bytes_per_step": nbytes_out, "ms_per_step": e2e_s * 1e3 / args.steps,
            "link": link,
+           "host_misfit_ms": statistics.median(mis_t), "host_threads": torch.get_num_threads(),
            "how": "pipelined calls (j3g_batched_*_async): each step's forward is queued two "
-                  "steps ahead; copies on their own streams overlap the products",
+                  "steps ahead, the gradient two steps back is waited for (three host buffer "
+                  "sets); copies on their own streams (in and out per direction) overlap the "
+                  "products",
            "blocking": {"value": units * world * args.steps / sync_s / 1e6,
                         "how": "j3g_batched_forward / j3g_batched_lqderivative, one at a time"}}
 

@@ -249,8 +249,10 @@ int j3g_batched_lqderivative(j3g_context *ctx, int nmodels, const double *h_mode
                              const double *h_misfits, double *h_grads);
 /* Pipelined host-buffer forms: the call queues the copy of its inputs in,
  * the product and the copy of its output back, and returns a ticket; the
- * copies run on two streams of the context's own (in, out), so they overlap
- * the products of the calls before and after.  j3g_batched_wait(ticket)
+ * copies run on streams of the context's own, one in and one out per
+ * direction (forward, derivative), so they overlap the products of the calls
+ * before and after, and a forward's data or a derivative's misfits do not
+ * queue behind the other direction's model-sized copies.  j3g_batched_wait(ticket)
  * blocks until that call's output is in host memory.  Up to four calls are
  * in flight (a fifth waits for the first: enough to queue a forward two
  * steps ahead of the misfit it feeds).  A call's product is replayed from a

@@ -106,9 +106,10 @@ struct j3g_context {
   DevBuf rmaps, rcoarse, rfine;
   RefineMaps rm{};
 
-  // pipelined host-buffer products (j3g_batched_*_async): inputs copied in on
-  // one stream, outputs out on another, the products on the context's stream;
-  // a ring of device slots lets one call's copies overlap another call's work
+  // pipelined host-buffer products (j3g_batched_*_async): inputs copied in and
+  // outputs out on copy streams of the call's direction, the products on the
+  // context's stream; a ring of device slots lets one call's copies overlap
+  // another call's work
   struct Slot {
     DevBuf in, in2, out;
     cudaEvent_t h2d = nullptr, done = nullptr, d2h = nullptr;
@@ -125,7 +126,11 @@ struct j3g_context {
   };
   static constexpr int kSlots = 4;
   Slot slots[kSlots];
-  cudaStream_t h2d_stream = nullptr, d2h_stream = nullptr;
+  // copy streams per direction (forward, derivative): a forward's data (a few
+  // MB) does not queue behind a derivative's gradients (the size of the
+  // models) on the way out, nor a derivative's misfits behind a forward's
+  // models on the way in
+  cudaStream_t h2d_stream[2] = {nullptr, nullptr}, d2h_stream[2] = {nullptr, nullptr};
   long long next_ticket = 0;
   // failure codes of calls whose slot was reused before they were waited for
   std::map<long long, int> failed_tickets;
@@ -1125,8 +1130,10 @@ int j3g_destroy(j3g_context *c) {
       if (g) cudaGraphExecDestroy(g);
     if (sl.flag) cudaFreeHost(sl.flag);
   }
-  if (c->h2d_stream) cudaStreamDestroy(c->h2d_stream);
-  if (c->d2h_stream) cudaStreamDestroy(c->d2h_stream);
+  for (int d = 0; d < 2; ++d) {
+    if (c->h2d_stream[d]) cudaStreamDestroy(c->h2d_stream[d]);
+    if (c->d2h_stream[d]) cudaStreamDestroy(c->d2h_stream[d]);
+  }
   for (auto &t : c->timed) {
     cudaEventDestroy(t.second.first);
     cudaEventDestroy(t.second.second);
@@ -1494,10 +1501,11 @@ namespace {
 // The next slot of the pipeline ring, its previous call complete; the copy
 // streams and events are made on first use.
 int pipeline_slot(j3g_context *c, j3g_context::Slot *&slot) {
-  if (!c->h2d_stream) {
-    J3G_CUDA(c, cudaStreamCreateWithFlags(&c->h2d_stream, cudaStreamNonBlocking));
-    J3G_CUDA(c, cudaStreamCreateWithFlags(&c->d2h_stream, cudaStreamNonBlocking));
-  }
+  for (int d = 0; d < 2; ++d)
+    if (!c->h2d_stream[d]) {
+      J3G_CUDA(c, cudaStreamCreateWithFlags(&c->h2d_stream[d], cudaStreamNonBlocking));
+      J3G_CUDA(c, cudaStreamCreateWithFlags(&c->d2h_stream[d], cudaStreamNonBlocking));
+    }
   slot = &c->slots[c->next_ticket % j3g_context::kSlots];
   if (!slot->h2d) {
     J3G_CUDA(c, cudaEventCreateWithFlags(&slot->h2d, cudaEventDisableTiming));
@@ -1519,8 +1527,8 @@ int pipeline_slot(j3g_context *c, j3g_context::Slot *&slot) {
 }
 
 // Queue the copies around a product: inputs (host -> slot buffers) on the
-// H2D stream, the product on the context's stream once they are in, the
-// output back on the D2H stream once the product is done.
+// direction's H2D stream, the product on the context's stream once they are
+// in, the output back on the direction's D2H stream once the product is done.
 struct PipeCopy {
   const double *host;
   DevBuf *dev;
@@ -1577,26 +1585,26 @@ int pipeline_product(j3g_context *c, j3g_context::Slot *slot, int dir, int nmod,
 int pipeline_run(j3g_context *c, j3g_context::Slot *slot, int dir, int nmod,
                  std::initializer_list<PipeCopy> ins, double *h_out, size_t n_out,
                  long long *ticket, const std::function<int(void)> &product) {
+  cudaStream_t h2d = c->h2d_stream[dir], d2h = c->d2h_stream[dir];
   for (const PipeCopy &in : ins) {
     if (!in.host) continue;
     J3G_TRY(ensure(c, *in.dev, sizeof(double) * in.n));
     J3G_CUDA(c, cudaMemcpyAsync(in.dev->p, in.host, sizeof(double) * in.n,
-                                cudaMemcpyHostToDevice, c->h2d_stream));
+                                cudaMemcpyHostToDevice, h2d));
   }
   J3G_TRY(ensure(c, slot->out, sizeof(double) * n_out));
-  J3G_CUDA(c, cudaEventRecord(slot->h2d, c->h2d_stream));
+  J3G_CUDA(c, cudaEventRecord(slot->h2d, h2d));
   J3G_CUDA(c, cudaStreamWaitEvent(c->stream, slot->h2d, 0));
   J3G_TRY(pipeline_product(c, slot, dir, nmod, product));
   J3G_CUDA(c, cudaEventRecord(slot->done, c->stream));
-  J3G_CUDA(c, cudaStreamWaitEvent(c->d2h_stream, slot->done, 0));
+  J3G_CUDA(c, cudaStreamWaitEvent(d2h, slot->done, 0));
   J3G_CUDA(c, cudaMemcpyAsync(h_out, slot->out.p, sizeof(double) * n_out, cudaMemcpyDeviceToHost,
-                              c->d2h_stream));
+                              d2h));
   // the error flag of the bounded waits, as it stands after this product
   *slot->flag = 0;
   if (c->gerr.p)
-    J3G_CUDA(c, cudaMemcpyAsync(slot->flag, c->gerr.p, sizeof(int), cudaMemcpyDeviceToHost,
-                                c->d2h_stream));
-  J3G_CUDA(c, cudaEventRecord(slot->d2h, c->d2h_stream));
+    J3G_CUDA(c, cudaMemcpyAsync(slot->flag, c->gerr.p, sizeof(int), cudaMemcpyDeviceToHost, d2h));
+  J3G_CUDA(c, cudaEventRecord(slot->d2h, d2h));
   slot->ticket = c->next_ticket++;
   if (ticket) *ticket = slot->ticket;
   return J3G_OK;
