@@ -221,6 +221,65 @@ def test_pipelined_calls_replay_graphs(ctx):
     run(s2, m2, rng.normal(size=(200, s2.stations.shape[0] * 9)))
 
 
+@pytest.mark.parametrize("transform", [W.T_NONE, W.T_FTG_INVARIANT])
+def test_pipelined_step_loop(ctx, transform):
+    """The inversion-step loop over pipelined calls -- each forward queued two
+    steps ahead, the misfit formed on the host from the step's data, its
+    derivative queued, the gradient of two steps back waited for, three
+    sets of page-locked buffers -- gives every step's data and gradient bit
+    for bit as the blocking calls do.  A forward's data and a derivative's
+    misfits travel on copy streams of their own direction while the other
+    direction's copies are in flight."""
+    import torch
+    kind = W.JOINT if transform == W.T_NONE else W.TENSOR
+    s = small_survey(kind, seed=296 + transform, transform=transform, nx=12, ny=10, nz=8,
+                     nmeas=30)
+    W.setup_context(ctx, s)
+    ctx.build_sensitivity(capi.STORE_F16X2)
+    rng = np.random.default_rng(37)
+    nmod, nd, nsteps = 40, s.stations.shape[0] * s.dpm, 9
+    batches = [s.model[None, :] * rng.uniform(0.5, 1.5, (nmod, s.nparm)) for _ in range(nsteps)]
+    obs = rng.normal(size=nd) * 1e-5
+    w = rng.uniform(0.5, 2.0, size=nd)
+
+    def pinned(shape):
+        return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    # each step's models stay as they are until its derivative is waited for
+    # (the FTG invariant's derivative reads them): one page-locked array each
+    models = [pinned((nmod, s.nparm)) for _ in range(nsteps)]
+    for m, b in zip(models, batches):
+        m[:] = b
+    sets = [dict(data=pinned((nmod, nd)), mis=pinned((nmod, nd)), grads=pinned((nmod, s.nparm)))
+            for _ in range(3)]
+    got_data, got_grads, mis_of = {}, {}, {}
+    fwd, adj = {}, {}
+
+    def queue_fwd(i):
+        fwd[i] = ctx.batched_forward_async(models[i], out=sets[i % 3]["data"])
+
+    def take_grad(i):
+        ctx.batched_wait(adj[i])
+        got_grads[i] = sets[i % 3]["grads"].copy()
+    for i in range(2):
+        queue_fwd(i)
+    for i in range(nsteps):
+        st = sets[i % 3]
+        ctx.batched_wait(fwd[i])
+        got_data[i] = st["data"].copy()
+        np.multiply(st["data"] - obs, w, out=st["mis"])
+        mis_of[i] = st["mis"].copy()
+        adj[i] = ctx.batched_lqderivative_async(models[i], st["mis"], out=st["grads"])
+        if i + 2 < nsteps:
+            queue_fwd(i + 2)
+        if i >= 2:
+            take_grad(i - 2)
+    for i in range(nsteps - 2, nsteps):
+        take_grad(i)
+    for i in range(nsteps):
+        assert np.array_equal(got_data[i], ctx.batched_forward(batches[i])), i
+        assert np.array_equal(got_grads[i], ctx.batched_lqderivative(batches[i], mis_of[i])), i
+
+
 def test_pinned_gemm_plans(ctx, oracle_lib):
     """Pinned plans (j3g_set_gemm_plan) are used as given -- the CTA pair with
     many K splits, one-SM 128-wide tiles -- and agree with the oracle; a tile
