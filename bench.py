@@ -516,6 +516,41 @@ def measure_netcdf(s, data):
     return out
 
 
+def pipelined_steps(ctx, sets, nsteps, misfit, nsets=3, back=2):
+    """The end-to-end loop over the pipelined host-buffer calls
+    (j3g_batched_forward_async / _lqderivative_async / j3g_batched_wait).
+
+    Step i waits for its own data, forms the misfit on the host (``misfit(st)``
+    reads st["data"] and writes st["mis"]), queues its derivative and then the
+    forward of step i + 2 (the batches' models are known ahead, as for
+    independent batches); the gradient of step i - ``back`` is taken (waited
+    for) last, before its host buffers come round again (``nsets`` sets of
+    arrays "models", "data", "mis", "grads").  With back = 1 the host waited
+    there until that gradient (268 MB) had come back, so the forward of step
+    i + 3 was queued late and waited for its models; back = 2 needs three
+    sets, or the misfit of step i + 1 overwrites what the derivative of step
+    i - 1 may still be reading.  The library's ring holds four calls (a fifth
+    waits for the oldest)."""
+    fwd, adj = {}, {}
+
+    def queue_fwd(i):
+        st = sets[i % nsets]
+        fwd[i] = ctx.batched_forward_async(st["models"], out=st["data"])
+    for i in range(min(2, nsteps)):
+        queue_fwd(i)
+    for i in range(nsteps):
+        st = sets[i % nsets]
+        ctx.batched_wait(fwd[i])
+        misfit(st)
+        adj[i] = ctx.batched_lqderivative_async(st["models"], st["mis"], out=st["grads"])
+        if i + 2 < nsteps:
+            queue_fwd(i + 2)
+        if i >= back:
+            ctx.batched_wait(adj[i - back])
+    for i in range(max(0, nsteps - back), nsteps):
+        ctx.batched_wait(adj[i])
+
+
 def run_batched(args, rank, world, local):
     import torch
     from jif3d_gb300 import capi, workloads as W
@@ -677,34 +712,12 @@ def run_batched(args, rank, world, local):
             ctx.batched_lqderivative(st["models"].numpy(), st["mis"].numpy(),
                                      out=st["grads"].numpy())
 
-    def e2e_pipelined(nsteps):
-        """Step i waits for its own data, forms the misfit, queues its
-        derivative and then the forward of step i + 2 (the batches' models are
-        known ahead, as for independent batches); the gradient of step i - 2
-        is taken (waited for) last, before its host buffers come round again
-        (three sets).  Waiting for the gradient of step i - 1 there instead
-        held the host until that gradient (268 MB) had come back, so the
-        forward of step i + 3 was queued late and waited for its models.  At
-        most four calls are in flight."""
-        fwd, adj = {}, {}
+    # the same buffers as numpy arrays for the pipelined calls, with their
+    # torch views for the misfit
+    np_sets = [dict({k: v.numpy() for k, v in st.items()}, torch=st) for st in sets]
 
-        def queue_fwd(i):
-            st = sets[i % 3]
-            fwd[i] = ctx.batched_forward_async(st["models"].numpy(), out=st["data"].numpy())
-        for i in range(min(2, nsteps)):
-            queue_fwd(i)
-        for i in range(nsteps):
-            st = sets[i % 3]
-            ctx.batched_wait(fwd[i])
-            host_misfit(st)
-            adj[i] = ctx.batched_lqderivative_async(st["models"].numpy(), st["mis"].numpy(),
-                                                    out=st["grads"].numpy())
-            if i + 2 < nsteps:
-                queue_fwd(i + 2)
-            if i >= 2:
-                ctx.batched_wait(adj[i - 2])
-        for i in range(max(0, nsteps - 2), nsteps):
-            ctx.batched_wait(adj[i])
+    def e2e_pipelined(nsteps):
+        pipelined_steps(ctx, np_sets, nsteps, lambda st: host_misfit(st["torch"]))
 
     # warm-up: each ring slot replays its product from a CUDA graph once the
     # same shape has run there twice; a run of K steps takes 2K tickets of the
