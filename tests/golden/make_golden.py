@@ -13,9 +13,9 @@
   spacing and the range of MeasPosX / MeasPosY), taken from the notebook's
   stored output.
 
-Run here, where the reference sources exist:
+Run where the reference sources exist:
     python tests/golden/make_golden.py <path/to/jif3D>
-The GPU machine has no reference tree; tests there read the committed JSON.
+Machines without the reference tree run the tests on the committed files.
 """
 import json
 import os
