@@ -154,21 +154,6 @@ __global__ void k_forward_reduce_raw(int nmeas, int nblk, const double *__restri
 }
 
 // ---------------------------------------------------------------------------
-// Background layers, one thread per station, layers in order (the running top
-// is accumulated exactly as the reference accumulates it).
-__device__ void tensor_box9(double mx, double my, double mz, double cx, double cy, double cz,
-                            double sx, double sy, double sz, double *u) {
-  u[0] = uxx_box(mx, my, mz, cx, cy, cz, sx, sy, sz);
-  u[4] = uxx_box(my, mx, mz, cy, cx, cz, sy, sx, sz);
-  u[8] = uxx_box(mz, mx, my, cz, cx, cy, sz, sx, sy);
-  u[1] = uxy_box(mx, my, mz, cx, cy, cz, sx, sy, sz);
-  u[3] = u[1];
-  u[2] = uxy_box(mx, mz, my, cx, cz, cy, sx, sz, sy);
-  u[6] = u[2];
-  u[5] = uxy_box(mz, my, mx, cz, cy, cx, sz, sy, sx);
-  u[7] = u[5];
-}
-
 // Background layer terms (GravityBackground.cpp:24-137).  A block takes 32
 // stations of one layer; warp k evaluates one prism component (g_z, Uxx, Uyy,
 // Uzz, Uxy, Uxz, Uyz; the eighth warp idles) for those 32 stations, each an
