@@ -635,11 +635,10 @@ __global__ void k_splitk_reduce(const float *__restrict__ P, int nsplit, long lo
 // consecutive threads read consecutive float4s -- and U splits at a time:
 // for a few splits G = 2 quads x 2 splits (four loads per thread, twice the
 // threads of four quads: 108 instead of 115 us for the 2-split adjoint of
-// 256 x 131072 outputs), for many 1 quad x 8 splits with the next batch
-// loading while one is added up.  The
-// split sums accumulate as unevaluated FP32 pairs
-// (hi + lo, error-free two-sum), about 48 bits -- as good as an FP64 sum of
-// FP32 partials -- without the FP64 pipe.  With more than kPairSplits splits
+// 256 x 131072 outputs), for many 1 quad x 4 splits with the next batch
+// loading while one is added up.  The split sums accumulate as unevaluated
+// FP32 pairs (hi + lo, error-free two-sum), about 48 bits -- as good as an
+// FP64 sum of FP32 partials -- without the FP64 pipe.  With more than kPairSplits splits
 // one FP64 add per output widens the pair; with fewer the pair is rounded to
 // FP32 first (relative 2^-24, below the FP32 rounding each partial already
 // carries) so that the pass stays at HBM speed: one FP64 operation per output
@@ -1170,7 +1169,7 @@ cudaError_t launch_splitk_reduce(const float *P, int nsplit, long long slice, in
   const bool fpow2 = factor != 0.0 && std::frexp(factor, &kf) == 0.5;  // factor = 2^(kf-1)
   if (fpow2 && nrow % 4 == 0 && ldp % 4 == 0 && slice % 4 == 0 && nmod <= 65535 &&
       (reinterpret_cast<uintptr_t>(P) & 15) == 0) {
-    if (nsplit > kPairSplits) {  // many splits: one quad per thread, 8 splits per batch
+    if (nsplit > kPairSplits) {  // many splits: one quad per thread, 4 splits per batch
       dim3 grid(cdiv(nrow / 4, (long long)kT), nmod);
       k_splitk_reduce4<true, 1><<<grid, kT, 0, st>>>(P, nsplit, slice, nrow, ldp, rowscale,
                                                      modscale, sexp, modmean, rowsum, kf - 1,
