@@ -727,11 +727,11 @@ def run_batched(args, rank, world, local):
         e2e_pipelined(args.steps)
     e2e_blocking(2)
     barrier(world)
-    # three timed runs of K steps each way: the median is reported, all listed
+    # five timed runs of K steps each way: the median is reported, all listed
     # (the host link is shared with the machine's other work, and single runs
-    # of a few tens of ms vary)
+    # of a few tens of ms now and then take twice as long)
     sync_runs, pipe_runs = [], []
-    for _ in range(3):
+    for _ in range(5):
         t0 = time.perf_counter()
         e2e_blocking(args.steps)
         t1 = time.perf_counter()
@@ -765,7 +765,7 @@ def run_batched(args, rank, world, local):
            "how": "pipelined calls (j3g_batched_*_async): each step's forward is queued two "
                   "steps ahead, the gradient two steps back is waited for (three host buffer "
                   "sets); copies on their own streams (in and out per direction) overlap the "
-                  "products; median of three timed runs of K steps",
+                  "products; median of five timed runs of K steps",
            "blocking": {"value": units * world * args.steps / sync_s / 1e6,
                         "runs_ms_per_step": [x * 1e3 / args.steps for x in sync_runs],
                         "how": "j3g_batched_forward / j3g_batched_lqderivative, one at a time"}}
